@@ -1,0 +1,232 @@
+/*
+ * graph_link_gb300 — C ABI of the GB300 (sm_103a) Personalized-PageRank engine.
+ *
+ * Plain extern "C" functions over raw device pointers, sizes and a
+ * cudaStream_t.  No torch types cross this boundary.  Every function returns a
+ * status code (GL_OK == 0); gl_last_error() gives the text of the last failure
+ * on the calling thread.  Outputs are owned by the caller.  Nothing here
+ * synchronizes the stream unless its comment says so.
+ *
+ * The reference (Dayan135/Page_Rank, package graph_link) has no C ABI: its
+ * native layer is the pybind11 module `graph_link_core`.  Each entry point
+ * below names the reference function or kernel launcher it replaces.
+ */
+#ifndef GRAPH_LINK_GB300_H
+#define GRAPH_LINK_GB300_H
+
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define GL_OK                    0
+#define GL_ERR_INVALID_ARGUMENT  1  /* maps to ValueError                      */
+#define GL_ERR_UNSUPPORTED_BLOCK 2  /* maps to ValueError (pbr_kernel.cu:392)  */
+#define GL_ERR_OOM               3  /* maps to MemoryError / RuntimeError      */
+#define GL_ERR_CUDA              4  /* maps to RuntimeError                    */
+#define GL_ERR_TIMEOUT           5  /* bounded device wait gave up             */
+#define GL_ERR_NONCANONICAL      6  /* CSR row not strictly increasing         */
+#define GL_ERR_WORKSPACE         7  /* workspace too small                     */
+
+/* ---- element types ------------------------------------------------------ */
+#define GL_I32 0
+#define GL_I64 1
+#define GL_F32 0
+#define GL_F64 1
+
+/* Text of the last error raised on the calling thread ("" when none). */
+const char* gl_last_error(void);
+/* ABI version of this library (major * 100 + minor). */
+int gl_version(void);
+
+/*
+ * A PBR matrix resident in device memory.  Field meaning follows the
+ * reference's pbr_matrix_t (Backend/graph_link/pbr_matrix/pbr_matrix.hpp:98-167)
+ * and the seven tensors its `.to()` uploads (graph_link/__init__.py:43-51):
+ * block codes as int64 bit patterns, int32 (row0, col0) coordinate pairs,
+ * int32 offsets into block_data (num_blocks + 1 entries), packed values in
+ * row-major bit order, and a CSR remainder with int32 indices.
+ *
+ * stripe_block_ptr has no reference counterpart: entry s is the first block
+ * of stripe s (blocks are stored stripe-major, as the reference builder emits
+ * them), with ceil(rows / block_rows) + 1 entries.  gl_pbr_stripe_index()
+ * derives it from block_coords.
+ */
+typedef struct gl_pbr_matrix {
+    int64_t rows, cols;
+    int32_t block_rows, block_cols;
+    int64_t num_blocks, packed_nnz, remainder_nnz;
+    int32_t value_type;                 /* GL_F32 or GL_F64                  */
+    const int64_t* block_codes;         /* [num_blocks]                      */
+    const int32_t* block_coords;        /* [2 * num_blocks]                  */
+    const int32_t* block_offsets;       /* [num_blocks + 1]                  */
+    const void*    block_data;          /* [packed_nnz]                      */
+    const int32_t* remainder_indptr;    /* [rows + 1]                        */
+    const int32_t* remainder_col_ind;   /* [remainder_nnz]                   */
+    const void*    remainder_data;      /* [remainder_nnz]                   */
+    const int32_t* stripe_block_ptr;    /* [ceil(rows/block_rows) + 1]       */
+} gl_pbr_matrix;
+
+/* ======================================================================== */
+/* PBR builder on the device                                                */
+/* Replaces csr_to_pbr<index_t, scalar_t> (pbr_matrix/pbr_matrix.cpp:340-477,
+ * bound at bindings/bindings.cpp:70-73).  Output is bit-identical to the
+ * reference builder for canonical CSR input (sorted, duplicate-free rows),
+ * including the order of the blocks inside each stripe.                    */
+/* ======================================================================== */
+typedef struct gl_pbr_build_counts {
+    int64_t num_blocks;          /* kept blocks                              */
+    int64_t packed_nnz;          /* length of block_data                     */
+    int64_t remainder_nnz;       /* length of remainder_col_ind / _data      */
+    int64_t max_stripe_blocks;   /* most distinct blocks in one stripe       */
+    int64_t distinct_blocks;     /* distinct blocks over all stripes         */
+} gl_pbr_build_counts;
+
+/* Device workspace (bytes) the two build phases need. */
+int64_t gl_pbr_build_workspace_bytes(int64_t rows, int64_t cols, int64_t nnz,
+                                     int32_t block_rows, int32_t block_cols);
+
+/* Phase 1: validates the CSR (indices in range, rows strictly increasing),
+ * counts blocks / packed values / remainder entries per stripe and row and
+ * scans them.  Synchronizes `stream` to return the totals in *counts.
+ * index_type: GL_I32 or GL_I64 for indptr and indices.
+ * Errors: GL_ERR_INVALID_ARGUMENT (block_rows * block_cols > 64, an index out
+ * of range, min_nnz outside 0..255), GL_ERR_NONCANONICAL, GL_ERR_WORKSPACE. */
+int gl_pbr_build_count(const void* indptr, const void* indices, int32_t index_type,
+                       int64_t rows, int64_t cols, int64_t nnz,
+                       int32_t block_rows, int32_t block_cols, int32_t min_nnz_per_block,
+                       void* workspace, int64_t workspace_bytes,
+                       gl_pbr_build_counts* counts, cudaStream_t stream);
+
+/* Phase 2: writes the PBR arrays.  Index outputs use index_type (the
+ * reference's PBRMatrixInt32* / PBRMatrixInt64* variants), values use
+ * value_type.  block_codes receives the raw 64-bit masks.  stripe_block_ptr
+ * (int32, ceil(rows/block_rows)+1 entries) may be NULL.  Must follow
+ * gl_pbr_build_count with the same arguments and workspace. */
+int gl_pbr_build_fill(const void* indptr, const void* indices, const void* values,
+                      int32_t index_type, int32_t value_type,
+                      int64_t rows, int64_t cols, int64_t nnz,
+                      int32_t block_rows, int32_t block_cols, int32_t min_nnz_per_block,
+                      void* workspace, int64_t workspace_bytes,
+                      const gl_pbr_build_counts* counts,
+                      uint64_t* block_codes, void* block_coords, void* block_offsets,
+                      void* block_data, void* remainder_indptr, void* remainder_col_ind,
+                      void* remainder_data, int32_t* stripe_block_ptr, cudaStream_t stream);
+
+/* Derives stripe_block_ptr from block_coords for PBR arrays built elsewhere
+ * (e.g. uploaded from the reference builder) and checks that the blocks are
+ * stripe-major.  flag_scratch: one device int32.  Synchronizes `stream`.
+ * Errors: GL_ERR_INVALID_ARGUMENT when blocks are not stripe-major. */
+int gl_pbr_stripe_index(const int32_t* block_coords, int64_t num_blocks, int64_t rows,
+                        int32_t block_rows, int32_t* stripe_block_ptr,
+                        int32_t* flag_scratch, cudaStream_t stream);
+
+/* ======================================================================== */
+/* Fused PBR-block + CSR-remainder SpMM                                     */
+/* Replaces pbr_spmm_cuda_dispatch (bindings/bindings_kernels.cu:13-83) and
+ * the kernels it launches, launch_pbr_spmm (kernels/pbr_kernel.cu:336-396)
+ * and launch_csr_spmm (kernels/pbr_kernel.cu:460-478).  One launch, no
+ * atomics, no second stream; Y is overwritten (no pre-zeroing needed).      */
+/* ======================================================================== */
+/* X: [batch][cols][features], Y: [batch][rows][features], both contiguous,
+ * element type A->value_type.  Supported blocks: 2x2, 4x4, 8x8 (others give
+ * GL_ERR_UNSUPPORTED_BLOCK, as the reference throws std::invalid_argument). */
+int gl_pbr_spmm(const gl_pbr_matrix* A, const void* X, void* Y,
+                int64_t batch, int64_t features, cudaStream_t stream);
+
+/* ======================================================================== */
+/* Personalized PageRank                                                    */
+/* ======================================================================== */
+/*
+ * Teleport (personalization) vectors, indexed by stripe so the fused
+ * iteration can add them in its epilogue.  Entry e puts weight[e] on
+ * (row[e], column col[e]); stripe s owns entries stripe_ptr[s] .. stripe_ptr[s+1].
+ */
+typedef struct gl_teleport {
+    const int32_t* stripe_ptr;   /* [ceil(rows/block_rows) + 1] */
+    const int32_t* row;          /* [num_entries]               */
+    const int32_t* col;          /* [num_entries]               */
+    const float*   weight;       /* [num_entries]               */
+    int64_t num_entries;
+} gl_teleport;
+
+/* Builds a gl_teleport from per-column seed sets (column k has seeds
+ * seed_idx[seed_ptr[k] .. seed_ptr[k+1]) ).  seed_weight NULL gives each
+ * seed of column k the weight 1/|S_k| (uniform personalization over the set;
+ * the reference's one-seed-per-column case, init_ppr_sources_kernel at
+ * kernels/ppr_kernel.cu:199-209, is |S_k| = 1).  Outputs: stripe_ptr
+ * (num_stripes + 1), row/col/weight (num_seeds).  counter_scratch: device
+ * int32[num_stripes + 1].  Errors: GL_ERR_INVALID_ARGUMENT for a seed outside
+ * [0, rows) — checked on the device and reported after a stream sync. */
+int gl_ppr_teleport_index(int64_t rows, int32_t block_rows, int64_t num_columns,
+                          const int32_t* seed_ptr, const int32_t* seed_idx,
+                          const float* seed_weight, int64_t num_seeds,
+                          int32_t* stripe_ptr, int32_t* row, int32_t* col, float* weight,
+                          int32_t* counter_scratch, cudaStream_t stream);
+
+/* X0 = teleport vectors (zero elsewhere), plus the dangling mass of X0 per
+ * column into dangling0[K] (double, accumulated: zero it first) when
+ * dangling_bitmap is not NULL.  Replaces launch_init_ppr
+ * (kernels/ppr_kernel.cu:211-216).  X0: [rows][K] of value_type. */
+int gl_ppr_init(const gl_teleport* tp, int64_t rows, int64_t K, int32_t value_type,
+                void* X0, const uint32_t* dangling_bitmap, double* dangling0,
+                cudaStream_t stream);
+
+/* Dangling mass of a given X per column: out[k] += sum over rows i with
+ * bit i set in dangling_bitmap of X[i][k] (for warm starts). */
+int gl_ppr_dangling_mass(const void* X, int64_t rows, int64_t K, int32_t value_type,
+                         const uint32_t* dangling_bitmap, double* out, cudaStream_t stream);
+
+#define GL_PPR_STOP_ALL        0  /* stop every column when max_k residual < tol */
+#define GL_PPR_STOP_PER_COLUMN 1  /* freeze column k once its residual < tol     */
+
+/*
+ * One fused power-iteration step (SpMM + alpha-scaling + teleport + dangling
+ * mass + per-column L1 residual in one pass):
+ *
+ *   X_out[:, k] = alpha * A X_in[:, k] + ((1 - alpha) + alpha * d_t[k]) * v_k
+ *   residual[t][k] = sum_i |X_out[i, k] - X_in[i, k]|
+ *   d_{t+1}[k]     = sum over dangling rows i of X_out[i, k]
+ *
+ * where v_k is the teleport vector of column k and d_t the dangling mass of
+ * X_in (zero when dangling_bitmap is NULL — the column-stochastic case of the
+ * reference update, ppr_update_normalized_kernel at kernels/ppr_kernel.cu:
+ * 130-168; with the bitmap it is the missing-mass update of
+ * batched_ppr_update_kernel, kernels/ppr_kernel.cu:57-97).
+ *
+ * The iteration number is t = *chunk_base + step_in_chunk, read on the device
+ * so a CUDA graph of several steps can be replayed.  residual_hist is
+ * [max_iterations][K] doubles and dangling_hist [max_iterations + 1][K]
+ * doubles, both zeroed before the first step; step t accumulates row t of
+ * residual_hist and row t + 1 of dangling_hist and reads row t of
+ * dangling_hist.  A step is a no-op when t >= max_iterations, or (STOP_ALL)
+ * when max_k residual_hist[t-1][k] < tol.  Under STOP_PER_COLUMN, a column
+ * whose residual_hist[t-1][k] < tol is copied unchanged and adds 0.
+ */
+typedef struct gl_ppr_step_params {
+    double  alpha;
+    double  tol;
+    int32_t stop_mode;
+    int32_t max_iterations;
+    int32_t step_in_chunk;
+    const int32_t*  chunk_base;       /* device int32                        */
+    double*         residual_hist;    /* device [max_iterations][K]          */
+    double*         dangling_hist;    /* device [max_iterations + 1][K]      */
+    const uint32_t* dangling_bitmap;  /* device, ceil(rows/32) words, or NULL */
+} gl_ppr_step_params;
+
+int gl_ppr_step(const gl_pbr_matrix* A, const gl_teleport* tp,
+                const void* X_in, void* X_out, int64_t K,
+                const gl_ppr_step_params* params, cudaStream_t stream);
+
+/* Adds `delta` to the device int32 at `counter` (stream-ordered; the node
+ * that advances chunk_base at the end of a captured chunk of steps). */
+int gl_counter_add(int32_t* counter, int32_t delta, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GRAPH_LINK_GB300_H */

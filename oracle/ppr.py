@@ -1,0 +1,68 @@
+"""FP64 Personalized-PageRank oracles — test infrastructure only.
+
+* :func:`power_iteration_fp64` restates the reference power iteration
+  (``Backend/graph_link/graph_link/__init__.py:242-271``) with the update of
+  ``ppr_update_normalized_kernel`` (``kernels/ppr_kernel.cu:130-168``):
+  ``X <- alpha * A X + (1 - alpha) * V`` and the stop rule "largest per-column
+  L1 change < tol", or, with ``dangling`` set, the missing-mass update of
+  ``batched_ppr_update_kernel`` (``kernels/ppr_kernel.cu:57-97``) generalised to
+  a teleport matrix V: the mass of dangling columns returns through V.
+* :func:`direct_solve_fp64` solves the fixed point exactly for small n:
+  ``(I - alpha * (A + V d^T)) x = (1 - alpha) v`` per column.
+* :func:`teleport_matrix` builds V from per-column seed sets (uniform weights).
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+
+def teleport_matrix(n: int, seed_sets) -> np.ndarray:
+    V = np.zeros((n, len(seed_sets)), dtype=np.float64)
+    for k, seeds in enumerate(seed_sets):
+        seeds = np.asarray(seeds, dtype=np.int64)
+        np.add.at(V[:, k], seeds, 1.0 / len(seeds))
+    return V
+
+
+def dangling_mask(A: sp.csr_matrix) -> np.ndarray:
+    """Columns without any stored entry."""
+    present = np.zeros(A.shape[1], dtype=bool)
+    present[A.indices] = True
+    return ~present
+
+
+def power_iteration_fp64(A: sp.csr_matrix, V: np.ndarray, alpha: float, max_iterations: int,
+                         tol: float, dangling: np.ndarray | None = None, x0: np.ndarray | None = None):
+    """Returns (X, iterations, converged, history)."""
+    A64 = A.astype(np.float64).tocsr()
+    X = V.copy() if x0 is None else np.asarray(x0, dtype=np.float64).copy()
+    history = []
+    for t in range(max_iterations):
+        Y = A64 @ X
+        Xn = alpha * Y + (1.0 - alpha) * V
+        if dangling is not None:
+            d = X[dangling].sum(axis=0)
+            Xn += alpha * d[None, :] * V
+        err = np.abs(Xn - X).sum(axis=0)
+        X = Xn
+        history.append(float(err.max()))
+        if err.max() < tol:
+            return X, t + 1, True, history
+    return X, max_iterations, False, history
+
+
+def direct_solve_fp64(A: sp.csr_matrix, V: np.ndarray, alpha: float,
+                      dangling: np.ndarray | None = None) -> np.ndarray:
+    n = A.shape[0]
+    A64 = A.astype(np.float64).tocsc()
+    X = np.zeros_like(V, dtype=np.float64)
+    for k in range(V.shape[1]):
+        v = V[:, k]
+        M = sp.identity(n, format="csc") - alpha * A64
+        if dangling is not None and dangling.any():
+            d = sp.csr_matrix(dangling.astype(np.float64)[None, :])
+            M = M - alpha * sp.csc_matrix(sp.csr_matrix(v[:, None]) @ d)
+        X[:, k] = spla.spsolve(M.tocsc(), (1.0 - alpha) * v)
+    return X

@@ -1,0 +1,311 @@
+// C ABI: error text, SpMM entry point, stripe index, and the personalized
+// PageRank entry points (teleport index, init, fused step).
+#include <cstdarg>
+#include <cstdio>
+
+#include "gl_common.cuh"
+#include "gl_scan.cuh"
+#include "stripe_kernel.cuh"
+
+namespace gl {
+
+namespace {
+thread_local char g_last_error[1024] = {0};
+}
+
+void set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+}
+
+const char* last_error() { return g_last_error; }
+
+namespace {
+
+int check_matrix(const gl_pbr_matrix* A) {
+    GL_REQUIRE(A != nullptr, GL_ERR_INVALID_ARGUMENT, "matrix descriptor is NULL");
+    GL_REQUIRE(A->rows >= 0 && A->cols >= 0, GL_ERR_INVALID_ARGUMENT, "negative matrix size");
+    GL_REQUIRE(A->value_type == GL_F32 || A->value_type == GL_F64, GL_ERR_INVALID_ARGUMENT,
+               "value_type must be GL_F32 or GL_F64");
+    const bool ok_block = (A->block_rows == A->block_cols) &&
+                          (A->block_rows == 2 || A->block_rows == 4 || A->block_rows == 8);
+    GL_REQUIRE(ok_block, GL_ERR_UNSUPPORTED_BLOCK,
+               "Unsupported block size for PBR SpMM. Only 2x2, 4x4, and 8x8 are supported.");
+    GL_REQUIRE(A->rows == 0 || (A->stripe_block_ptr && A->remainder_indptr), GL_ERR_INVALID_ARGUMENT,
+               "stripe_block_ptr / remainder_indptr are NULL");
+    return GL_OK;
+}
+
+template <typename S>
+StripeArgs<S> make_args(const gl_pbr_matrix* A) {
+    StripeArgs<S> a{};
+    a.codes = A->block_codes;
+    a.coords = A->block_coords;
+    a.offsets = A->block_offsets;
+    a.bdata = static_cast<const S*>(A->block_data);
+    a.rem_ptr = A->remainder_indptr;
+    a.rem_col = A->remainder_col_ind;
+    a.rem_val = static_cast<const S*>(A->remainder_data);
+    a.stripe_ptr = A->stripe_block_ptr;
+    a.rows = A->rows;
+    a.cols = A->cols;
+    a.nstripes = ceil_div(A->rows, A->block_rows);
+    a.batch = 1;
+    return a;
+}
+
+__global__ void stripe_index_kernel(const int32_t* coords, int64_t nb, int64_t rows, int br, int64_t ns,
+                                    int32_t* ptr, int32_t* flag) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b > nb) return;
+    int64_t s_cur;
+    if (b < nb) {
+        const int64_t r0 = coords[2 * b];
+        if (r0 < 0 || r0 >= rows || r0 % br != 0) {
+            atomicOr(flag, 1);
+            return;
+        }
+        s_cur = r0 / br;
+    } else {
+        s_cur = ns;
+    }
+    int64_t s_prev = -1;
+    if (b > 0) {
+        const int64_t rp = coords[2 * (b - 1)];
+        s_prev = (rp >= 0 && rp < rows) ? rp / br : -1;
+    }
+    if (s_cur < s_prev) {
+        atomicOr(flag, 1);
+        return;
+    }
+    for (int64_t s = s_prev + 1; s <= s_cur; ++s) ptr[s] = (int32_t)b;
+}
+
+__global__ void teleport_count_kernel(int64_t K, const int32_t* seed_ptr, const int32_t* seed_idx, int64_t rows,
+                                      int br, int32_t* counters, int64_t ns, int32_t* stripe_ptr, int32_t* row,
+                                      int32_t* col, float* weight, const float* seed_w, bool scatter) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    const int32_t e0 = seed_ptr[k], e1 = seed_ptr[k + 1];
+    const float uni = e1 > e0 ? 1.0f / (float)(e1 - e0) : 0.0f;
+    for (int32_t e = e0; e < e1; ++e) {
+        const int64_t r = seed_idx[e];
+        if (r < 0 || r >= rows) {
+            atomicOr(&counters[ns], 1);
+            continue;
+        }
+        const int64_t s = r / br;
+        if (!scatter) {
+            atomicAdd(&counters[s], 1);
+        } else {
+            const int32_t slot = stripe_ptr[s] + atomicAdd(&counters[s], 1);
+            row[slot] = (int32_t)r;
+            col[slot] = (int32_t)k;
+            weight[slot] = seed_w ? seed_w[e] : uni;
+        }
+    }
+}
+
+template <typename S>
+__global__ void ppr_init_kernel(const int32_t* row, const int32_t* col, const float* w, int64_t n, int64_t K, S* X,
+                                const uint32_t* bitmap, double* d0) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const int64_t r = row[e], k = col[e];
+    atomicAdd(X + r * K + k, (S)w[e]);
+    if (bitmap && ((bitmap[r >> 5] >> (r & 31)) & 1u)) atomicAdd(d0 + k, (double)w[e]);
+}
+
+template <typename S>
+__global__ void dangling_mass_kernel(const S* X, int64_t rows, int64_t K, const uint32_t* bitmap, double* out,
+                                     int64_t rows_per_block) {
+    const int64_t k = (int64_t)blockIdx.y * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    const int64_t r0 = (int64_t)blockIdx.x * rows_per_block;
+    const int64_t r1 = r0 + rows_per_block < rows ? r0 + rows_per_block : rows;
+    double acc = 0.0;
+    for (int64_t r = r0; r < r1; ++r)
+        if ((bitmap[r >> 5] >> (r & 31)) & 1u) acc += (double)X[r * K + k];
+    if (acc != 0.0) atomicAdd(out + k, acc);
+}
+
+__global__ void counter_add_kernel(int32_t* c, int32_t d) { *c += d; }
+
+}  // namespace
+}  // namespace gl
+
+using namespace gl;
+
+extern "C" const char* gl_last_error(void) { return last_error(); }
+extern "C" int gl_version(void) { return 100; }
+
+extern "C" int gl_pbr_spmm(const gl_pbr_matrix* A, const void* X, void* Y, int64_t batch, int64_t features,
+                           cudaStream_t stream) {
+    int rc = check_matrix(A);
+    if (rc != GL_OK) return rc;
+    GL_REQUIRE(batch >= 0 && features >= 0, GL_ERR_INVALID_ARGUMENT, "negative batch / features");
+    GL_REQUIRE(features < (int64_t)INT32_MAX, GL_ERR_INVALID_ARGUMENT, "too many features");
+    if (batch == 0 || features == 0 || A->rows == 0) return GL_OK;
+    GL_REQUIRE(X != nullptr && Y != nullptr, GL_ERR_INVALID_ARGUMENT, "X / Y is NULL");
+    if (A->value_type == GL_F32) {
+        StripeArgs<float> a = make_args<float>(A);
+        a.batch = batch;
+        a.K = (int32_t)features;
+        a.X = static_cast<const float*>(X);
+        a.Y = static_cast<float*>(Y);
+        return launch_stripe<float, false>(a, A->block_rows, A->block_cols, stream);
+    }
+    StripeArgs<double> a = make_args<double>(A);
+    a.batch = batch;
+    a.K = (int32_t)features;
+    a.X = static_cast<const double*>(X);
+    a.Y = static_cast<double*>(Y);
+    return launch_stripe<double, false>(a, A->block_rows, A->block_cols, stream);
+}
+
+extern "C" int gl_pbr_stripe_index(const int32_t* block_coords, int64_t num_blocks, int64_t rows, int32_t block_rows,
+                                   int32_t* stripe_block_ptr, int32_t* flag_scratch, cudaStream_t stream) {
+    GL_REQUIRE(num_blocks >= 0 && rows >= 0 && block_rows >= 1, GL_ERR_INVALID_ARGUMENT, "bad sizes");
+    GL_REQUIRE(stripe_block_ptr && flag_scratch, GL_ERR_INVALID_ARGUMENT, "NULL output");
+    const int64_t ns = ceil_div(rows, block_rows);
+    GL_CUDA_TRY(cudaMemsetAsync(flag_scratch, 0, sizeof(int32_t), stream));
+    GL_CUDA_TRY(cudaMemsetAsync(stripe_block_ptr, 0, sizeof(int32_t) * (ns + 1), stream));
+    stripe_index_kernel<<<(unsigned)ceil_div(num_blocks + 1, 256), 256, 0, stream>>>(
+        block_coords, num_blocks, rows, block_rows, ns, stripe_block_ptr, flag_scratch);
+    GL_LAUNCH_CHECK("stripe_index_kernel");
+    int32_t flag = 0;
+    GL_CUDA_TRY(cudaMemcpyAsync(&flag, flag_scratch, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+    GL_CUDA_TRY(cudaStreamSynchronize(stream));
+    GL_REQUIRE(flag == 0, GL_ERR_INVALID_ARGUMENT,
+               "PBR blocks must be stored stripe-major with row origins that are multiples of block_rows");
+    return GL_OK;
+}
+
+extern "C" int gl_ppr_teleport_index(int64_t rows, int32_t block_rows, int64_t num_columns, const int32_t* seed_ptr,
+                                     const int32_t* seed_idx, const float* seed_weight, int64_t num_seeds,
+                                     int32_t* stripe_ptr, int32_t* row, int32_t* col, float* weight,
+                                     int32_t* counter_scratch, cudaStream_t stream) {
+    GL_REQUIRE(rows >= 0 && block_rows >= 1 && num_columns >= 0 && num_seeds >= 0, GL_ERR_INVALID_ARGUMENT,
+               "bad sizes");
+    GL_REQUIRE(stripe_ptr && counter_scratch, GL_ERR_INVALID_ARGUMENT, "NULL output");
+    const int64_t ns = ceil_div(rows, block_rows);
+    GL_CUDA_TRY(cudaMemsetAsync(counter_scratch, 0, sizeof(int32_t) * (ns + 1), stream));
+    const unsigned grid = (unsigned)ceil_div(num_columns > 0 ? num_columns : 1, 128);
+    if (num_columns > 0) {
+        teleport_count_kernel<<<grid, 128, 0, stream>>>(num_columns, seed_ptr, seed_idx, rows, block_rows,
+                                                        counter_scratch, ns, nullptr, nullptr, nullptr, nullptr,
+                                                        nullptr, false);
+        GL_LAUNCH_CHECK("teleport_count_kernel");
+    }
+    int32_t bad = 0;
+    GL_CUDA_TRY(cudaMemcpyAsync(&bad, counter_scratch + ns, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+    GL_CUDA_TRY(cudaStreamSynchronize(stream));
+    GL_REQUIRE(bad == 0, GL_ERR_INVALID_ARGUMENT, "seed node index out of range [0, %lld)", (long long)rows);
+    // Per-stripe counts -> stripe_ptr (exclusive scan).  The counters are
+    // free once copied, so they double as the scan's scratch (it needs at
+    // most ns + 1 elements).
+    {
+        GL_CUDA_TRY(cudaMemcpyAsync(stripe_ptr, counter_scratch, sizeof(int32_t) * ns, cudaMemcpyDeviceToDevice,
+                                    stream));
+        GL_CUDA_TRY(cudaMemsetAsync(stripe_ptr + ns, 0, sizeof(int32_t), stream));
+        int rc = exclusive_scan<int32_t, OpSum>(stripe_ptr, stripe_ptr, ns + 1, counter_scratch, 0, OpSum(), stream);
+        if (rc != GL_OK) return rc;
+    }
+    GL_CUDA_TRY(cudaMemsetAsync(counter_scratch, 0, sizeof(int32_t) * (ns + 1), stream));
+    if (num_columns > 0) {
+        teleport_count_kernel<<<grid, 128, 0, stream>>>(num_columns, seed_ptr, seed_idx, rows, block_rows,
+                                                        counter_scratch, ns, stripe_ptr, row, col, weight,
+                                                        seed_weight, true);
+        GL_LAUNCH_CHECK("teleport_count_kernel");
+    }
+    return GL_OK;
+}
+
+extern "C" int gl_ppr_init(const gl_teleport* tp, int64_t rows, int64_t K, int32_t value_type, void* X0,
+                           const uint32_t* dangling_bitmap, double* dangling0, cudaStream_t stream) {
+    GL_REQUIRE(tp != nullptr && rows >= 0 && K >= 0, GL_ERR_INVALID_ARGUMENT, "bad arguments");
+    GL_REQUIRE(value_type == GL_F32 || value_type == GL_F64, GL_ERR_INVALID_ARGUMENT, "bad value_type");
+    const size_t es = value_type == GL_F32 ? 4 : 8;
+    if (rows * K > 0) GL_CUDA_TRY(cudaMemsetAsync(X0, 0, es * rows * K, stream));
+    if (tp->num_entries == 0) return GL_OK;
+    const unsigned grid = (unsigned)ceil_div(tp->num_entries, 256);
+    const uint32_t* bm = dangling0 ? dangling_bitmap : nullptr;
+    if (value_type == GL_F32)
+        ppr_init_kernel<float><<<grid, 256, 0, stream>>>(tp->row, tp->col, tp->weight, tp->num_entries, K,
+                                                         static_cast<float*>(X0), bm, dangling0);
+    else
+        ppr_init_kernel<double><<<grid, 256, 0, stream>>>(tp->row, tp->col, tp->weight, tp->num_entries, K,
+                                                          static_cast<double*>(X0), bm, dangling0);
+    GL_LAUNCH_CHECK("ppr_init_kernel");
+    return GL_OK;
+}
+
+extern "C" int gl_ppr_dangling_mass(const void* X, int64_t rows, int64_t K, int32_t value_type,
+                                    const uint32_t* dangling_bitmap, double* out, cudaStream_t stream) {
+    GL_REQUIRE(rows >= 0 && K >= 0 && dangling_bitmap && out, GL_ERR_INVALID_ARGUMENT, "bad arguments");
+    if (rows == 0 || K == 0) return GL_OK;
+    const int64_t rpb = 4096;
+    dim3 grid((unsigned)ceil_div(rows, rpb), (unsigned)ceil_div(K, 128));
+    if (value_type == GL_F32)
+        dangling_mass_kernel<float><<<grid, 128, 0, stream>>>(static_cast<const float*>(X), rows, K, dangling_bitmap,
+                                                              out, rpb);
+    else
+        dangling_mass_kernel<double><<<grid, 128, 0, stream>>>(static_cast<const double*>(X), rows, K,
+                                                               dangling_bitmap, out, rpb);
+    GL_LAUNCH_CHECK("dangling_mass_kernel");
+    return GL_OK;
+}
+
+extern "C" int gl_ppr_step(const gl_pbr_matrix* A, const gl_teleport* tp, const void* X_in, void* X_out, int64_t K,
+                           const gl_ppr_step_params* p, cudaStream_t stream) {
+    int rc = check_matrix(A);
+    if (rc != GL_OK) return rc;
+    GL_REQUIRE(tp != nullptr && p != nullptr, GL_ERR_INVALID_ARGUMENT, "NULL teleport / params");
+    GL_REQUIRE(A->rows == A->cols, GL_ERR_INVALID_ARGUMENT, "PPR needs a square matrix");
+    GL_REQUIRE(K >= 0 && K < (int64_t)INT32_MAX, GL_ERR_INVALID_ARGUMENT, "bad K");
+    GL_REQUIRE(p->chunk_base && p->residual_hist && p->dangling_hist, GL_ERR_INVALID_ARGUMENT,
+               "NULL iteration buffers");
+    GL_REQUIRE(p->stop_mode == GL_PPR_STOP_ALL || p->stop_mode == GL_PPR_STOP_PER_COLUMN, GL_ERR_INVALID_ARGUMENT,
+               "bad stop_mode");
+    GL_REQUIRE(X_in != X_out, GL_ERR_INVALID_ARGUMENT, "X_in and X_out must be different buffers");
+    if (K == 0 || A->rows == 0) return GL_OK;
+    GL_REQUIRE(tp->num_entries == 0 || tp->stripe_ptr, GL_ERR_INVALID_ARGUMENT, "teleport index missing");
+#define GL_FILL_PPR(a)                                     \
+    (a).batch = 1;                                         \
+    (a).K = (int32_t)K;                                    \
+    (a).tp_ptr = tp->stripe_ptr;                           \
+    (a).tp_row = tp->row;                                  \
+    (a).tp_col = tp->col;                                  \
+    (a).tp_w = tp->weight;                                 \
+    (a).alpha = p->alpha;                                  \
+    (a).tol = p->tol;                                      \
+    (a).stop_mode = p->stop_mode;                          \
+    (a).max_iter = p->max_iterations;                      \
+    (a).step = p->step_in_chunk;                           \
+    (a).chunk_base = p->chunk_base;                        \
+    (a).res_hist = p->residual_hist;                       \
+    (a).dang_hist = p->dangling_hist;                      \
+    (a).dbitmap = p->dangling_bitmap
+    if (A->value_type == GL_F32) {
+        StripeArgs<float> a = make_args<float>(A);
+        GL_FILL_PPR(a);
+        a.X = static_cast<const float*>(X_in);
+        a.Y = static_cast<float*>(X_out);
+        return launch_stripe<float, true>(a, A->block_rows, A->block_cols, stream);
+    }
+    StripeArgs<double> a = make_args<double>(A);
+    GL_FILL_PPR(a);
+    a.X = static_cast<const double*>(X_in);
+    a.Y = static_cast<double*>(X_out);
+    return launch_stripe<double, true>(a, A->block_rows, A->block_cols, stream);
+#undef GL_FILL_PPR
+}
+
+extern "C" int gl_counter_add(int32_t* counter, int32_t delta, cudaStream_t stream) {
+    GL_REQUIRE(counter != nullptr, GL_ERR_INVALID_ARGUMENT, "NULL counter");
+    counter_add_kernel<<<1, 1, 0, stream>>>(counter, delta);
+    GL_LAUNCH_CHECK("counter_add_kernel");
+    return GL_OK;
+}

@@ -1,0 +1,98 @@
+// Shared helpers for the sm_103a PPR / PBR kernels: status codes, the
+// per-thread last-error string and small device utilities.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "graph_link_gb300.h"
+
+namespace gl {
+
+// Per-thread last error text returned by gl_last_error().
+void set_error(const char* fmt, ...);
+const char* last_error();
+
+// Maps a CUDA runtime error to a status code and records its text.
+inline int cuda_status(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return GL_OK;
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? GL_ERR_OOM : GL_ERR_CUDA;
+}
+
+#define GL_CUDA_TRY(expr)                                                   \
+    do {                                                                    \
+        cudaError_t _e = (expr);                                            \
+        if (_e != cudaSuccess) return ::gl::cuda_status(_e, #expr);         \
+    } while (0)
+
+#define GL_LAUNCH_CHECK(what)                                               \
+    do {                                                                    \
+        cudaError_t _e = cudaGetLastError();                                \
+        if (_e != cudaSuccess) return ::gl::cuda_status(_e, what);          \
+    } while (0)
+
+#define GL_REQUIRE(cond, code, ...)                                         \
+    do {                                                                    \
+        if (!(cond)) { ::gl::set_error(__VA_ARGS__); return (code); }       \
+    } while (0)
+
+inline int num_sms() {
+    static int cached = 0;
+    if (cached == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev);
+        if (cached <= 0) cached = 152;
+    }
+    return cached;
+}
+
+__host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Warp-wide reductions.
+__device__ __forceinline__ int64_t warp_min_i64(int64_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        int64_t w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w < v ? w : v;
+    }
+    return v;
+}
+__device__ __forceinline__ int64_t warp_max_i64(int64_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        int64_t w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+__device__ __forceinline__ uint64_t warp_or_u64(uint64_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v |= __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ int warp_sum_i32(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ int64_t warp_sum_i64(int64_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+// Inclusive scan over the warp.
+__device__ __forceinline__ int64_t warp_incl_scan_i64(int64_t v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int64_t w = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += w;
+    }
+    return v;
+}
+
+}  // namespace gl

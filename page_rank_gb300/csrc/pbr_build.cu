@@ -1,0 +1,593 @@
+// PBR builder on the device (sm_103a): CSR -> 64-bit block bitmasks, packed
+// values and a CSR remainder, bit-identical to the reference builder
+// csr_to_pbr<index_t, scalar_t> (Backend/graph_link/pbr_matrix/pbr_matrix.cpp:
+// 340-477) for canonical CSR input.
+//
+// Work split: one warp per stripe (block_rows consecutive rows).  Lane r walks
+// row r of the stripe; because each row is column-sorted, the warp merges the
+// rows by block column (warp-min of the lanes' head block columns), which
+// yields the stripe's distinct blocks in block-column order together with
+// their bitmask, the CSR position of their first nonzero, and per-row counts.
+//
+// Three device passes:
+//   count  — per stripe: distinct / kept blocks, packed values; per row:
+//            remainder entries; CSR validation (range, strictly increasing);
+//   (scans of those counts; an exclusive running max of distinct blocks)
+//   fill   — per stripe: record the blocks, reproduce the reference's emit
+//            order (below), write codes / coords / offsets, then merge once
+//            more to move the values into block_data or the remainder.
+//
+// Emit order.  The reference emits a stripe's kept blocks in the iteration
+// order of a std::unordered_map<index_t, ...> keyed by the block index
+// (truncated to index_t), constructed with a bucket hint of
+// sqrt(number of column blocks) and clear()ed — which keeps its bucket array —
+// after every stripe (pbr_matrix.cpp:374-376, 389, 402, 425).  That order is a
+// deterministic function of the keys' insertion order and the bucket count:
+//   * the hash of an integer key is the key itself (sign-extended to size_t),
+//     the bucket is hash % bucket_count;
+//   * a node inserted into an empty bucket goes to the front of the node
+//     list; one inserted into a non-empty bucket goes to the front of that
+//     bucket's run.  So with insertion times tau, the list is ordered by
+//     (first tau of the node's bucket, descending) then (tau, descending);
+//   * a rehash happens just before the insertion that would take the element
+//     count to (last bucket count + 1) and re-inserts the existing nodes in
+//     their list order — i.e. it renumbers tau by list position;
+//   * bucket counts only grow, and clear() keeps them, so the bucket count a
+//     stripe starts with depends only on the most elements any earlier stripe
+//     held.
+// The sequence of bucket counts is read, on the host, from the same standard
+// library container (filled with dummy keys), so no prime table is assumed.
+// The same standard library must build this library and the reference.
+
+#include <cmath>
+#include <cstring>
+#include <unordered_map>
+#include <vector>
+
+#include "gl_common.cuh"
+#include "gl_scan.cuh"
+
+namespace gl {
+namespace {
+
+constexpr int kBuildThreads = 256;
+constexpr int kBuildWarps = kBuildThreads / 32;
+constexpr int kMaxChain = 64;
+constexpr int64_t kInf = INT64_MAX;
+
+enum BuildFlag { kFlagRange = 0, kFlagNoncanon = 1, kFlagIndptr = 2, kNumFlags = 4 };
+
+// Workspace layout (every region 256-byte aligned).
+struct BuildWs {
+    int32_t* flags;         // kNumFlags
+    int64_t* stripe_m;      // nstripes + 1 : distinct blocks   -> exclusive scan
+    int64_t* stripe_kept;   // nstripes + 1 : kept blocks       -> exclusive scan
+    int64_t* stripe_packed; // nstripes + 1 : kept values       -> exclusive scan
+    int64_t* stripe_prefmax;// nstripes + 1 : exclusive running max of stripe_m
+    int64_t* row_rem;       // rows + 1     : remainder entries -> exclusive scan
+    int64_t* chain;         // 2 * kMaxChain: (count, buckets) pairs
+    int64_t* scan_scratch;  // scan_scratch_elems(max(nstripes, rows) + 1)
+    // per distinct block (upper bound: nnz), indexed by stripe_m scan
+    uint64_t* rec_code;
+    int64_t*  rec_bcol;
+    int32_t*  rec_ins;      // first-nonzero position, then insertion rank
+    int32_t*  rec_tau;
+    uint32_t* rec_bkt;
+    int32_t*  rec_g;        // bucket-run head tau, later: data offset
+    int32_t*  rec_pos;      // list position, later: output slot (-1 = dropped)
+    int64_t bytes;
+};
+
+inline int64_t align256(int64_t x) { return (x + 255) & ~int64_t(255); }
+
+BuildWs layout_ws(void* base, int64_t rows, int64_t nnz, int32_t br) {
+    BuildWs w{};
+    const int64_t ns = ceil_div(rows, br);
+    const int64_t scan_n = scan_scratch_elems((ns > rows ? ns : rows) + 1);
+    char* p = static_cast<char*>(base);
+    int64_t off = 0;
+    auto take = [&](int64_t bytes) { char* q = p ? p + off : nullptr; off += align256(bytes); return q; };
+    w.flags = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * kNumFlags));
+    w.stripe_m = reinterpret_cast<int64_t*>(take(8 * (ns + 1)));
+    w.stripe_kept = reinterpret_cast<int64_t*>(take(8 * (ns + 1)));
+    w.stripe_packed = reinterpret_cast<int64_t*>(take(8 * (ns + 1)));
+    w.stripe_prefmax = reinterpret_cast<int64_t*>(take(8 * (ns + 1)));
+    w.row_rem = reinterpret_cast<int64_t*>(take(8 * (rows + 1)));
+    w.chain = reinterpret_cast<int64_t*>(take(8 * 2 * kMaxChain));
+    w.scan_scratch = reinterpret_cast<int64_t*>(take(8 * scan_n));
+    const int64_t nr = nnz > 0 ? nnz : 1;
+    w.rec_code = reinterpret_cast<uint64_t*>(take(8 * nr));
+    w.rec_bcol = reinterpret_cast<int64_t*>(take(8 * nr));
+    w.rec_ins = reinterpret_cast<int32_t*>(take(4 * nr));
+    w.rec_tau = reinterpret_cast<int32_t*>(take(4 * nr));
+    w.rec_bkt = reinterpret_cast<uint32_t*>(take(4 * nr));
+    w.rec_g = reinterpret_cast<int32_t*>(take(4 * nr));
+    w.rec_pos = reinterpret_cast<int32_t*>(take(4 * nr));
+    w.bytes = off;
+    return w;
+}
+
+// ---------------------------------------------------------------------------
+// Warp merge of the rows of one stripe.  Lanes 0..br-1 hold a cursor into
+// their row.  step() advances to the next distinct block column and returns
+// (for every lane) the block column, the lane's first position and count in
+// that block, and the block's code / first position over the whole stripe.
+// ---------------------------------------------------------------------------
+template <typename I>
+struct StripeMerge {
+    const I* indices;
+    int64_t p, end;          // this lane's cursor into its row
+    int64_t row_start;
+    int64_t prev_col;
+    int br, bc, lane;
+    bool check;
+    int bad_range, bad_order, bad_indptr;
+
+    // Cursors are clamped to [0, nnz] so a malformed indptr cannot cause an
+    // out-of-bounds read; the count pass flags it and the build is rejected.
+    __device__ void init(const I* indptr, const I* idx, int64_t s, int64_t rows, int64_t nnz, int br_, int bc_,
+                         bool chk) {
+        indices = idx;
+        br = br_;
+        bc = bc_;
+        lane = threadIdx.x & 31;
+        check = chk;
+        bad_range = 0;
+        bad_order = 0;
+        bad_indptr = 0;
+        const int64_t row = s * br + lane;
+        if (lane < br && row < rows) {
+            const int64_t a = (int64_t)indptr[row];
+            const int64_t b = (int64_t)indptr[row + 1];
+            if (a < 0 || b < a || b > nnz) bad_indptr = 1;
+            if (row == 0 && a != 0) bad_indptr = 1;
+            if (row + 1 == rows && b != nnz) bad_indptr = 1;
+            p = a < 0 ? 0 : (a > nnz ? nnz : a);
+            end = b < p ? p : (b > nnz ? nnz : b);
+        } else {
+            p = 0;
+            end = 0;
+        }
+        row_start = p;
+        prev_col = -1;
+    }
+
+    // Returns false when the stripe is exhausted.
+    __device__ bool step(int64_t cols, int64_t& bcol, uint64_t& code, int64_t& first,
+                         int& my_count, int64_t& my_first) {
+        const int64_t head = (p < end) ? (int64_t)indices[p] / bc : kInf;
+        const int64_t cur = warp_min_i64(head);
+        if (cur == kInf) return false;
+        uint64_t bits = 0;
+        int cnt = 0;
+        int64_t f = kInf;
+        if (head == cur) {
+            f = p;
+            while (p < end) {
+                const int64_t col = (int64_t)indices[p];
+                if (col / bc != cur) break;
+                if (check) {
+                    if (col < 0 || col >= cols) bad_range = 1;
+                    if (col <= prev_col) bad_order = 1;
+                }
+                prev_col = col;
+                const int64_t bit = (int64_t)lane * bc + col % bc;
+                if (bit >= 0 && bit < 64) bits |= 1ull << bit;
+                ++cnt;
+                ++p;
+            }
+        }
+        bcol = cur;
+        code = warp_or_u64(bits);
+        first = warp_min_i64(f);
+        my_count = cnt;
+        my_first = f;
+        return true;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// count: per stripe distinct / kept blocks and kept values; per row remainder
+// entries; validation flags.
+// ---------------------------------------------------------------------------
+template <typename I>
+__global__ void __launch_bounds__(kBuildThreads)
+build_count_kernel(const I* indptr, const I* indices, int64_t rows, int64_t cols, int64_t nnz, int br, int bc,
+                   int min_nnz, int64_t nstripes, BuildWs w) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp_id = (int64_t)blockIdx.x * kBuildWarps + (threadIdx.x >> 5);
+    const int64_t nwarps = (int64_t)gridDim.x * kBuildWarps;
+    for (int64_t s = warp_id; s < nstripes; s += nwarps) {
+        StripeMerge<I> mg;
+        mg.init(indptr, indices, s, rows, nnz, br, bc, true);
+        int64_t m = 0, kept = 0, packed = 0, rem = 0;
+        int64_t bcol, first, my_first;
+        uint64_t code;
+        int my_count;
+        int64_t last_bcol = -1;
+        while (mg.step(cols, bcol, code, first, my_count, my_first)) {
+            // A negative or out-of-order column makes block columns repeat;
+            // the count is still finite and the flags reject the build.
+            if (bcol <= last_bcol) mg.bad_order = 1;
+            last_bcol = bcol;
+            ++m;
+            const int pop = __popcll(code);
+            if (pop >= min_nnz) {
+                ++kept;
+                packed += pop;
+            } else {
+                rem += my_count;
+            }
+        }
+        if (lane == 0) {
+            w.stripe_m[s] = m;
+            w.stripe_kept[s] = kept;
+            w.stripe_packed[s] = packed;
+        }
+        const int64_t row = s * br + lane;
+        if (lane < br && row < rows) w.row_rem[row] = rem;
+        if (__any_sync(0xffffffffu, mg.bad_range) && lane == 0) atomicOr(&w.flags[kFlagRange], 1);
+        if (__any_sync(0xffffffffu, mg.bad_order) && lane == 0) atomicOr(&w.flags[kFlagNoncanon], 1);
+        if (__any_sync(0xffffffffu, mg.bad_indptr) && lane == 0) atomicOr(&w.flags[kFlagIndptr], 1);
+    }
+}
+
+__device__ __forceinline__ uint32_t key_bucket(int64_t key_value, bool key32, uint64_t buckets) {
+    // std::hash of an integer is the value converted to size_t.
+    const int64_t k = key32 ? (int64_t)(int32_t)(uint32_t)(uint64_t)key_value : key_value;
+    return (uint32_t)((uint64_t)k % buckets);
+}
+
+// Orders the first `present` records (by insertion rank) as the standard
+// library's node list would under `buckets`; writes list positions to rec_pos.
+__device__ void list_order(int64_t s, int64_t ncb, bool key32, uint64_t buckets, int m, int present,
+                           const int64_t* bcol, const int32_t* ins, const int32_t* tau, uint32_t* bkt,
+                           int32_t* g, int32_t* pos) {
+    const int lane = threadIdx.x & 31;
+    for (int e = lane; e < m; e += 32)
+        if (ins[e] < present) bkt[e] = key_bucket(s * ncb + bcol[e], key32, buckets);
+    __syncwarp();
+    for (int e = lane; e < m; e += 32) {
+        if (ins[e] >= present) continue;
+        int32_t head = tau[e];
+        const uint32_t be = bkt[e];
+        for (int f = 0; f < m; ++f)
+            if (ins[f] < present && bkt[f] == be && tau[f] < head) head = tau[f];
+        g[e] = head;
+    }
+    __syncwarp();
+    for (int e = lane; e < m; e += 32) {
+        if (ins[e] >= present) continue;
+        const int32_t ge = g[e], te = tau[e];
+        int r = 0;
+        for (int f = 0; f < m; ++f) {
+            if (ins[f] >= present) continue;
+            const int32_t gf = g[f];
+            if (gf > ge || (gf == ge && tau[f] > te)) ++r;
+        }
+        pos[e] = r;
+    }
+    __syncwarp();
+}
+
+template <typename I, typename S>
+__global__ void __launch_bounds__(kBuildThreads)
+build_fill_kernel(const I* indptr, const I* indices, const S* values, int64_t rows, int64_t cols, int64_t nnz,
+                  int br, int bc, int min_nnz, int64_t nstripes, int64_t ncb, bool key32, int nchain,
+                  BuildWs w, uint64_t* out_codes, I* out_coords, I* out_offsets, S* out_data,
+                  I* out_rem_col, S* out_rem_val, int32_t* out_stripe_ptr) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp_id = (int64_t)blockIdx.x * kBuildWarps + (threadIdx.x >> 5);
+    const int64_t nwarps = (int64_t)gridDim.x * kBuildWarps;
+    for (int64_t s = warp_id; s < nstripes; s += nwarps) {
+        const int64_t rbase = w.stripe_m[s];
+        const int m = (int)(w.stripe_m[s + 1] - rbase);
+        const int64_t kept_base = w.stripe_kept[s];
+        const int64_t packed_base = w.stripe_packed[s];
+        if (lane == 0 && out_stripe_ptr) out_stripe_ptr[s] = (int32_t)kept_base;
+        if (m == 0) continue;
+
+        uint64_t* code_r = w.rec_code + rbase;
+        int64_t* bcol_r = w.rec_bcol + rbase;
+        int32_t* ins_r = w.rec_ins + rbase;
+        int32_t* tau_r = w.rec_tau + rbase;
+        uint32_t* bkt_r = w.rec_bkt + rbase;
+        int32_t* g_r = w.rec_g + rbase;
+        int32_t* pos_r = w.rec_pos + rbase;
+
+        // 1. record the distinct blocks in block-column order
+        {
+            StripeMerge<I> mg;
+            mg.init(indptr, indices, s, rows, nnz, br, bc, false);
+            int64_t bcol, first, my_first;
+            uint64_t code;
+            int my_count;
+            int j = 0;
+            while (mg.step(cols, bcol, code, first, my_count, my_first)) {
+                if (lane == 0) {
+                    code_r[j] = code;
+                    bcol_r[j] = bcol;
+                    ins_r[j] = (int32_t)(first - (int64_t)indptr[s * br]);
+                }
+                ++j;
+            }
+        }
+        __syncwarp();
+        // 2. insertion rank = rank of the first-nonzero position
+        for (int e = lane; e < m; e += 32) {
+            const int32_t fe = ins_r[e];
+            int r = 0;
+            for (int f = 0; f < m; ++f) r += ins_r[f] < fe;
+            tau_r[e] = r;
+        }
+        __syncwarp();
+        for (int e = lane; e < m; e += 32) ins_r[e] = tau_r[e];
+        __syncwarp();
+        // 3. bucket count at stripe start, rehashes inside the stripe
+        const int64_t M = w.stripe_prefmax[s];
+        int J = 0;
+        while (J + 1 < nchain && w.chain[2 * (J + 1)] <= M) ++J;
+        while (J + 1 < nchain && w.chain[2 * (J + 1)] <= m) {
+            const int present = (int)(w.chain[2 * (J + 1)] - 1);
+            list_order(s, ncb, key32, (uint64_t)w.chain[2 * J + 1], m, present, bcol_r, ins_r, tau_r,
+                       bkt_r, g_r, pos_r);
+            for (int e = lane; e < m; e += 32)
+                if (ins_r[e] < present) tau_r[e] = pos_r[e];
+            __syncwarp();
+            ++J;
+        }
+        list_order(s, ncb, key32, (uint64_t)w.chain[2 * J + 1], m, m, bcol_r, ins_r, tau_r, bkt_r, g_r,
+                   pos_r);
+        // 4. output slot and data offset of each kept block, in list order
+        for (int e = lane; e < m; e += 32) {
+            const bool kept_e = __popcll(code_r[e]) >= min_nnz;
+            int slot = -1, doff = 0;
+            if (kept_e) {
+                slot = 0;
+                const int32_t pe = pos_r[e];
+                for (int f = 0; f < m; ++f) {
+                    const int pf = __popcll(code_r[f]);
+                    if (pf >= min_nnz && pos_r[f] < pe) {
+                        ++slot;
+                        doff += pf;
+                    }
+                }
+                const int64_t ob = kept_base + slot;
+                out_codes[ob] = code_r[e];
+                out_coords[2 * ob] = (I)(s * br);
+                out_coords[2 * ob + 1] = (I)(bcol_r[e] * bc);
+                out_offsets[ob] = (I)(packed_base + doff);
+            }
+            tau_r[e] = slot;
+            g_r[e] = doff;
+        }
+        __syncwarp();
+        // 5. merge again and move the values
+        {
+            StripeMerge<I> mg;
+            mg.init(indptr, indices, s, rows, nnz, br, bc, false);
+            const int64_t row = s * br + lane;
+            int64_t rem_cursor = (lane < br && row < rows) ? w.row_rem[row] : 0;
+            int64_t bcol, first, my_first;
+            uint64_t code;
+            int my_count;
+            int j = 0;
+            while (mg.step(cols, bcol, code, first, my_count, my_first)) {
+                const int slot = tau_r[j];
+                if (slot >= 0) {
+                    const int before = (int)warp_incl_scan_i64(my_count) - my_count;
+                    const int64_t dst = packed_base + g_r[j] + before;
+                    for (int i = 0; i < my_count; ++i) out_data[dst + i] = values[my_first + i];
+                } else {
+                    for (int i = 0; i < my_count; ++i) {
+                        out_rem_col[rem_cursor + i] = indices[my_first + i];
+                        out_rem_val[rem_cursor + i] = values[my_first + i];
+                    }
+                    rem_cursor += my_count;
+                }
+                ++j;
+            }
+        }
+    }
+}
+
+template <typename I>
+__global__ void finish_kernel(const BuildWs w, int64_t rows, int64_t nstripes, I* out_offsets,
+                              I* out_rem_indptr, int32_t* out_stripe_ptr) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i <= rows) out_rem_indptr[i] = (I)w.row_rem[i];
+    if (i == 0) {
+        out_offsets[w.stripe_kept[nstripes]] = (I)w.stripe_packed[nstripes];
+        if (out_stripe_ptr) out_stripe_ptr[nstripes] = (int32_t)w.stripe_kept[nstripes];
+        out_offsets[0] = (I)0;
+    }
+}
+
+int check_args(int32_t index_type, int64_t rows, int64_t cols, int64_t nnz, int32_t br, int32_t bc, int32_t min_nnz) {
+    GL_REQUIRE(index_type == GL_I32 || index_type == GL_I64, GL_ERR_INVALID_ARGUMENT, "index_type must be GL_I32 or GL_I64");
+    GL_REQUIRE(rows >= 0 && cols >= 0 && nnz >= 0, GL_ERR_INVALID_ARGUMENT, "negative matrix size");
+    GL_REQUIRE(br >= 1 && bc >= 1 && (int64_t)br * bc <= 64, GL_ERR_INVALID_ARGUMENT,
+               "block_rows * block_cols must be in 1..64 (got %d x %d)", br, bc);
+    GL_REQUIRE(br <= 32, GL_ERR_INVALID_ARGUMENT, "block_rows > 32 is not supported by the device builder");
+    GL_REQUIRE(min_nnz >= 0 && min_nnz <= 255, GL_ERR_INVALID_ARGUMENT, "min_nnz_per_block must be in 0..255");
+    GL_REQUIRE(nnz < (int64_t)INT32_MAX || index_type == GL_I64, GL_ERR_INVALID_ARGUMENT,
+               "nnz does not fit the int32 index type");
+    return GL_OK;
+}
+
+// Bucket counts the standard library's unordered_map goes through when built
+// with `hint` buckets and filled one key at a time, as (count, buckets) pairs;
+// the first pair is (0, initial buckets).
+int bucket_chain(uint64_t hint, int64_t max_elems, int64_t* pairs) {
+    std::unordered_map<int64_t, uint8_t> probe(static_cast<size_t>(hint));
+    int n = 0;
+    size_t last = probe.bucket_count();
+    pairs[0] = 0;
+    pairs[1] = (int64_t)last;
+    n = 1;
+    for (int64_t i = 0; i < max_elems; ++i) {
+        probe.emplace(i, 0);
+        if (probe.bucket_count() != last) {
+            last = probe.bucket_count();
+            if (n >= kMaxChain) return -1;
+            pairs[2 * n] = i + 1;
+            pairs[2 * n + 1] = (int64_t)last;
+            ++n;
+        }
+    }
+    return n;
+}
+
+template <typename I>
+int count_impl(const I* indptr, const I* indices, int64_t rows, int64_t cols, int64_t nnz, int32_t br, int32_t bc,
+               int32_t min_nnz, const BuildWs& w, gl_pbr_build_counts* counts, cudaStream_t stream) {
+    const int64_t ns = ceil_div(rows, br);
+    GL_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int32_t) * kNumFlags, stream));
+    {
+        // The trailing slot of every count array must be zero for the scans.
+        int64_t* regions[5] = {w.stripe_m, w.stripe_kept, w.stripe_packed, w.stripe_prefmax, w.row_rem};
+        const int64_t lens[5] = {ns + 1, ns + 1, ns + 1, ns + 1, rows + 1};
+        for (int i = 0; i < 5; ++i) GL_CUDA_TRY(cudaMemsetAsync(regions[i], 0, 8 * lens[i], stream));
+    }
+    if (ns > 0) {
+        int64_t blocks = ceil_div(ns, kBuildWarps);
+        const int64_t cap = (int64_t)num_sms() * 16;
+        if (blocks > cap) blocks = cap;
+        build_count_kernel<I><<<(unsigned)blocks, kBuildThreads, 0, stream>>>(indptr, indices, rows, cols, nnz, br,
+                                                                              bc, min_nnz, ns, w);
+        GL_LAUNCH_CHECK("build_count_kernel");
+    }
+    int rc;
+    // exclusive running max of distinct blocks per stripe (bucket state)
+    if ((rc = exclusive_scan<int64_t, OpMax>(w.stripe_m, w.stripe_prefmax, ns + 1, w.scan_scratch, int64_t(0),
+                                             OpMax(), stream)) != GL_OK)
+        return rc;
+    if ((rc = exclusive_scan<int64_t, OpSum>(w.stripe_m, w.stripe_m, ns + 1, w.scan_scratch, int64_t(0), OpSum(),
+                                             stream)) != GL_OK)
+        return rc;
+    if ((rc = exclusive_scan<int64_t, OpSum>(w.stripe_kept, w.stripe_kept, ns + 1, w.scan_scratch, int64_t(0),
+                                             OpSum(), stream)) != GL_OK)
+        return rc;
+    if ((rc = exclusive_scan<int64_t, OpSum>(w.stripe_packed, w.stripe_packed, ns + 1, w.scan_scratch, int64_t(0),
+                                             OpSum(), stream)) != GL_OK)
+        return rc;
+    if ((rc = exclusive_scan<int64_t, OpSum>(w.row_rem, w.row_rem, rows + 1, w.scan_scratch, int64_t(0), OpSum(),
+                                             stream)) != GL_OK)
+        return rc;
+    int32_t flags[kNumFlags];
+    int64_t tot[5];
+    GL_CUDA_TRY(cudaMemcpyAsync(flags, w.flags, sizeof(flags), cudaMemcpyDeviceToHost, stream));
+    GL_CUDA_TRY(cudaMemcpyAsync(&tot[0], w.stripe_kept + ns, 8, cudaMemcpyDeviceToHost, stream));
+    GL_CUDA_TRY(cudaMemcpyAsync(&tot[1], w.stripe_packed + ns, 8, cudaMemcpyDeviceToHost, stream));
+    GL_CUDA_TRY(cudaMemcpyAsync(&tot[2], w.row_rem + rows, 8, cudaMemcpyDeviceToHost, stream));
+    GL_CUDA_TRY(cudaMemcpyAsync(&tot[3], w.stripe_prefmax + ns, 8, cudaMemcpyDeviceToHost, stream));
+    GL_CUDA_TRY(cudaMemcpyAsync(&tot[4], w.stripe_m + ns, 8, cudaMemcpyDeviceToHost, stream));
+    GL_CUDA_TRY(cudaStreamSynchronize(stream));
+    GL_REQUIRE(!flags[kFlagIndptr], GL_ERR_INVALID_ARGUMENT,
+               "CSR indptr must start at 0, be non-decreasing and end at nnz=%lld", (long long)nnz);
+    GL_REQUIRE(!flags[kFlagRange], GL_ERR_INVALID_ARGUMENT, "CSR column index out of range [0, %lld)",
+               (long long)cols);
+    GL_REQUIRE(!flags[kFlagNoncanon], GL_ERR_NONCANONICAL,
+               "CSR rows must have strictly increasing column indices (sorted, no duplicates)");
+    GL_REQUIRE(tot[0] + tot[2] <= nnz && tot[1] + tot[2] == nnz, GL_ERR_INVALID_ARGUMENT,
+               "CSR indptr does not describe nnz=%lld entries", (long long)nnz);
+    GL_REQUIRE(tot[0] < (int64_t)INT32_MAX, GL_ERR_INVALID_ARGUMENT, "too many blocks for int32 stripe pointers");
+    counts->num_blocks = tot[0];
+    counts->packed_nnz = tot[1];
+    counts->remainder_nnz = tot[2];
+    counts->max_stripe_blocks = tot[3];
+    counts->distinct_blocks = tot[4];
+    return GL_OK;
+}
+
+template <typename I, typename S>
+int fill_impl(const I* indptr, const I* indices, const S* values, int64_t rows, int64_t cols, int64_t nnz, int32_t br,
+              int32_t bc,
+              int32_t min_nnz, const BuildWs& w, const gl_pbr_build_counts* counts, uint64_t* codes, I* coords,
+              I* offsets, S* data, I* rem_indptr, I* rem_col, S* rem_val, int32_t* stripe_ptr, cudaStream_t stream) {
+    const int64_t ns = ceil_div(rows, br);
+    const uint64_t ncb = (uint64_t)ceil_div(cols, bc);
+    const uint64_t hint = (uint64_t)std::sqrt((double)ncb);
+    int64_t chain[2 * kMaxChain];
+    const int nchain = bucket_chain(hint, counts->max_stripe_blocks, chain);
+    GL_REQUIRE(nchain > 0, GL_ERR_INVALID_ARGUMENT, "bucket chain longer than %d steps", kMaxChain);
+    GL_CUDA_TRY(cudaMemcpyAsync(w.chain, chain, sizeof(int64_t) * 2 * nchain, cudaMemcpyHostToDevice, stream));
+    if (ns > 0) {
+        int64_t blocks = ceil_div(ns, kBuildWarps);
+        const int64_t cap = (int64_t)num_sms() * 16;
+        if (blocks > cap) blocks = cap;
+        build_fill_kernel<I, S><<<(unsigned)blocks, kBuildThreads, 0, stream>>>(
+            indptr, indices, values, rows, cols, nnz, br, bc, min_nnz, ns, (int64_t)ncb, sizeof(I) == 4, nchain, w, codes,
+            coords, offsets, data, rem_col, rem_val, stripe_ptr);
+        GL_LAUNCH_CHECK("build_fill_kernel");
+    }
+    finish_kernel<I><<<(unsigned)ceil_div(rows + 1, 256), 256, 0, stream>>>(w, rows, ns, offsets, rem_indptr,
+                                                                            stripe_ptr);
+    GL_LAUNCH_CHECK("finish_kernel");
+    // The chain lives in host stack memory: make sure the copy finished.
+    GL_CUDA_TRY(cudaStreamSynchronize(stream));
+    return GL_OK;
+}
+
+}  // namespace
+}  // namespace gl
+
+using namespace gl;
+
+extern "C" int64_t gl_pbr_build_workspace_bytes(int64_t rows, int64_t cols, int64_t nnz, int32_t block_rows,
+                                                int32_t block_cols) {
+    (void)cols;
+    (void)block_cols;
+    if (rows < 0 || nnz < 0 || block_rows < 1) return -1;
+    return layout_ws(nullptr, rows, nnz, block_rows).bytes;
+}
+
+extern "C" int gl_pbr_build_count(const void* indptr, const void* indices, int32_t index_type, int64_t rows,
+                                  int64_t cols, int64_t nnz, int32_t block_rows, int32_t block_cols,
+                                  int32_t min_nnz_per_block, void* workspace, int64_t workspace_bytes,
+                                  gl_pbr_build_counts* counts, cudaStream_t stream) {
+    int rc = check_args(index_type, rows, cols, nnz, block_rows, block_cols, min_nnz_per_block);
+    if (rc != GL_OK) return rc;
+    GL_REQUIRE(counts != nullptr, GL_ERR_INVALID_ARGUMENT, "counts is NULL");
+    const BuildWs w = layout_ws(workspace, rows, nnz, block_rows);
+    GL_REQUIRE(workspace != nullptr && workspace_bytes >= w.bytes, GL_ERR_WORKSPACE,
+               "workspace of %lld bytes needed", (long long)w.bytes);
+    GL_REQUIRE(rows == 0 || indptr != nullptr, GL_ERR_INVALID_ARGUMENT, "indptr is NULL");
+    if (index_type == GL_I32)
+        return count_impl<int32_t>(static_cast<const int32_t*>(indptr), static_cast<const int32_t*>(indices), rows,
+                                   cols, nnz, block_rows, block_cols, min_nnz_per_block, w, counts, stream);
+    return count_impl<int64_t>(static_cast<const int64_t*>(indptr), static_cast<const int64_t*>(indices), rows, cols,
+                               nnz, block_rows, block_cols, min_nnz_per_block, w, counts, stream);
+}
+
+extern "C" int gl_pbr_build_fill(const void* indptr, const void* indices, const void* values, int32_t index_type,
+                                 int32_t value_type, int64_t rows, int64_t cols, int64_t nnz, int32_t block_rows,
+                                 int32_t block_cols, int32_t min_nnz_per_block, void* workspace,
+                                 int64_t workspace_bytes, const gl_pbr_build_counts* counts, uint64_t* block_codes,
+                                 void* block_coords, void* block_offsets, void* block_data, void* remainder_indptr,
+                                 void* remainder_col_ind, void* remainder_data, int32_t* stripe_block_ptr,
+                                 cudaStream_t stream) {
+    int rc = check_args(index_type, rows, cols, nnz, block_rows, block_cols, min_nnz_per_block);
+    if (rc != GL_OK) return rc;
+    GL_REQUIRE(value_type == GL_F32 || value_type == GL_F64, GL_ERR_INVALID_ARGUMENT, "value_type must be GL_F32 or GL_F64");
+    GL_REQUIRE(counts != nullptr, GL_ERR_INVALID_ARGUMENT, "counts is NULL");
+    const BuildWs w = layout_ws(workspace, rows, nnz, block_rows);
+    GL_REQUIRE(workspace != nullptr && workspace_bytes >= w.bytes, GL_ERR_WORKSPACE,
+               "workspace of %lld bytes needed", (long long)w.bytes);
+    GL_REQUIRE(block_offsets != nullptr && remainder_indptr != nullptr, GL_ERR_INVALID_ARGUMENT,
+               "block_offsets / remainder_indptr are NULL");
+#define GL_FILL(I, S)                                                                                             \
+    return fill_impl<I, S>(static_cast<const I*>(indptr), static_cast<const I*>(indices),                         \
+                           static_cast<const S*>(values), rows, cols, nnz, block_rows, block_cols, min_nnz_per_block, w, \
+                           counts, block_codes, static_cast<I*>(block_coords), static_cast<I*>(block_offsets),    \
+                           static_cast<S*>(block_data), static_cast<I*>(remainder_indptr),                       \
+                           static_cast<I*>(remainder_col_ind), static_cast<S*>(remainder_data), stripe_block_ptr, \
+                           stream)
+    if (index_type == GL_I32) {
+        if (value_type == GL_F32) GL_FILL(int32_t, float);
+        GL_FILL(int32_t, double);
+    }
+    if (value_type == GL_F32) GL_FILL(int64_t, float);
+    GL_FILL(int64_t, double);
+#undef GL_FILL
+}

@@ -1,0 +1,210 @@
+"""Device-side Personalized PageRank runs over a registered PBR matrix.
+
+One run owns two [rows, K] iterate buffers, a residual history
+[max_iterations, K] and a dangling-mass history [max_iterations + 1, K]
+(float64), and a device iteration counter.  Steps are launched in chunks;
+each step is one fused kernel (``gl_ppr_step``) that skips itself once the
+run has converged, so the host only synchronizes once per chunk instead of
+once per iteration (the reference syncs every iteration with ``.item()``,
+``graph_link/__init__.py:262``).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import native
+from .pbr import _ptr, matrix_desc
+
+
+@dataclass
+class Teleport:
+    """Teleport vectors indexed by stripe (see ``gl_teleport``)."""
+
+    stripe_ptr: torch.Tensor
+    row: torch.Tensor
+    col: torch.Tensor
+    weight: torch.Tensor
+    num_columns: int
+
+    def desc(self) -> native.TeleportDesc:
+        d = native.TeleportDesc()
+        d.stripe_ptr = _ptr(self.stripe_ptr)
+        d.row = _ptr(self.row)
+        d.col = _ptr(self.col)
+        d.weight = _ptr(self.weight)
+        d.num_entries = int(self.row.numel())
+        return d
+
+
+def teleport_from_seed_sets(seed_ptr: torch.Tensor, seed_idx: torch.Tensor, rows: int,
+                            block_rows: int, seed_weight: torch.Tensor | None = None) -> Teleport:
+    """Column k teleports to seeds ``seed_idx[seed_ptr[k]:seed_ptr[k+1]]``, each
+    with weight ``seed_weight`` (default 1/|set|)."""
+    dev = seed_idx.device
+    K = int(seed_ptr.numel()) - 1
+    n = int(seed_idx.numel())
+    ns = -(-rows // block_rows)
+    seed_ptr = seed_ptr.to(dev, torch.int32).contiguous()
+    seed_idx = seed_idx.to(dev, torch.int32).contiguous()
+    if seed_weight is not None:
+        seed_weight = seed_weight.to(dev, torch.float32).contiguous()
+    tp = Teleport(stripe_ptr=torch.empty(ns + 1, dtype=torch.int32, device=dev),
+                  row=torch.empty(n, dtype=torch.int32, device=dev),
+                  col=torch.empty(n, dtype=torch.int32, device=dev),
+                  weight=torch.empty(n, dtype=torch.float32, device=dev),
+                  num_columns=K)
+    scratch = torch.empty(ns + 1, dtype=torch.int32, device=dev)
+    native.check(native.lib().gl_ppr_teleport_index(
+        rows, block_rows, K, seed_ptr.data_ptr(), _ptr(seed_idx), _ptr(seed_weight), n,
+        tp.stripe_ptr.data_ptr(), _ptr(tp.row), _ptr(tp.col), _ptr(tp.weight),
+        scratch.data_ptr(), torch.cuda.current_stream(dev).cuda_stream))
+    return tp
+
+
+def dangling_bitmap(col_ind: torch.Tensor, rows: int) -> torch.Tensor:
+    """uint32 bitmap (as int32 tensor) of the columns with no stored entry.
+
+    For a column-normalized transition matrix those are the dangling nodes
+    (no out-edges), whose mass the dangling update sends to the teleport
+    vector."""
+    dev = col_ind.device
+    present = torch.zeros(rows, dtype=torch.bool, device=dev)
+    if col_ind.numel():
+        present[col_ind.long()] = True
+    dang = (~present).to(torch.int64)
+    words = -(-rows // 32)
+    pad = torch.zeros(words * 32, dtype=torch.int64, device=dev)
+    pad[:rows] = dang
+    weights = (torch.ones(32, dtype=torch.int64, device=dev) << torch.arange(32, device=dev))
+    packed = (pad.view(words, 32) * weights).sum(dim=1)
+    return packed.to(torch.int64).bitwise_and(0xFFFFFFFF).to(torch.int32) if words else \
+        torch.zeros(1, dtype=torch.int32, device=dev)
+
+
+@dataclass
+class PprResult:
+    X: torch.Tensor
+    iterations: int
+    converged: bool
+    history: list = field(default_factory=list)
+    column_iterations: np.ndarray | None = None
+
+
+class PprRun:
+    """State of one batched power iteration (K columns) over one matrix."""
+
+    def __init__(self, meta: dict, rows: int, cols: int, block_rows: int, block_cols: int,
+                 teleport: Teleport, alpha: float, max_iterations: int, tol: float,
+                 stop_mode: int = native.GL_PPR_STOP_ALL, dangling_bits: torch.Tensor | None = None):
+        if rows != cols:
+            raise ValueError("personalized PageRank needs a square matrix")
+        self.meta = meta
+        self.rows, self.cols = rows, cols
+        self.block_rows, self.block_cols = block_rows, block_cols
+        self.tp = teleport
+        self.K = teleport.num_columns
+        self.alpha = float(alpha)
+        self.max_iterations = int(max_iterations)
+        self.tol = float(tol)
+        self.stop_mode = stop_mode
+        self.dangling_bits = dangling_bits
+        dev = meta["data"].device
+        dtype = meta["data"].dtype
+        self.device = dev
+        self.bufs = [torch.empty((rows, self.K), dtype=dtype, device=dev),
+                     torch.empty((rows, self.K), dtype=dtype, device=dev)]
+        self.res_hist = torch.zeros((max(self.max_iterations, 1), self.K), dtype=torch.float64, device=dev)
+        self.dang_hist = torch.zeros((self.max_iterations + 1, self.K), dtype=torch.float64, device=dev)
+        self.chunk_base = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._desc = matrix_desc(meta, rows, cols, block_rows, block_cols)
+        self._tpd = teleport.desc()
+        self._vtype = native.GL_F32 if dtype == torch.float32 else native.GL_F64
+        self._params = []
+
+    def _stream(self) -> int:
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def init(self, x0: torch.Tensor | None = None) -> None:
+        L = native.lib()
+        st = self._stream()
+        dbits = _ptr(self.dangling_bits)
+        if x0 is None:
+            native.check(L.gl_ppr_init(self._tpd, self.rows, self.K, self._vtype,
+                                       self.bufs[0].data_ptr(), dbits,
+                                       self.dang_hist[0].data_ptr() if dbits else None, st))
+        else:
+            self.bufs[0].copy_(x0)
+            if dbits:
+                native.check(L.gl_ppr_dangling_mass(self.bufs[0].data_ptr(), self.rows, self.K,
+                                                    self._vtype, dbits, self.dang_hist[0].data_ptr(),
+                                                    st))
+
+    def _step_params(self, i: int) -> native.PprStepParams:
+        while len(self._params) <= i:
+            p = native.PprStepParams()
+            p.alpha = self.alpha
+            p.tol = self.tol
+            p.stop_mode = self.stop_mode
+            p.max_iterations = self.max_iterations
+            p.step_in_chunk = len(self._params)
+            p.chunk_base = self.chunk_base.data_ptr()
+            p.residual_hist = self.res_hist.data_ptr()
+            p.dangling_hist = self.dang_hist.data_ptr()
+            p.dangling_bitmap = _ptr(self.dangling_bits)
+            self._params.append(p)
+        return self._params[i]
+
+    def launch_chunk(self, n: int) -> None:
+        """Launch n (even) steps starting at the device counter, then advance it."""
+        L = native.lib()
+        st = self._stream()
+        for i in range(n):
+            native.check(L.gl_ppr_step(self._desc, self._tpd, self.bufs[i % 2].data_ptr(),
+                                       self.bufs[(i + 1) % 2].data_ptr(), self.K,
+                                       self._step_params(i), st))
+        native.check(L.gl_counter_add(self.chunk_base.data_ptr(), n, st))
+
+    def run(self, chunk: int = 8, x0: torch.Tensor | None = None) -> PprResult:
+        chunk = max(2, chunk + (chunk % 2))
+        self.init(x0)
+        history: list[float] = []
+        col_iter = np.full(self.K, -1, dtype=np.int64)
+        iterations = self.max_iterations
+        converged = False
+        done = 0
+        while done < self.max_iterations:
+            self.launch_chunk(chunk)
+            n = min(chunk, self.max_iterations - done)
+            res = self.res_hist[done:done + n].cpu().numpy()  # synchronizes the stream
+            finished = False
+            for t in range(n):
+                row = res[t]
+                history.append(float(row.max()) if self.K else 0.0)
+                newly = (col_iter < 0) & (row < self.tol)
+                col_iter[newly] = done + t + 1
+                if self.stop_mode == native.GL_PPR_STOP_ALL:
+                    if self.K and row.max() < self.tol:
+                        iterations = done + t + 1
+                        converged = True
+                        finished = True
+                        break
+                elif (col_iter >= 0).all():
+                    iterations = done + t + 1
+                    converged = True
+                    finished = True
+                    break
+            done += n
+            if finished:
+                break
+        if self.stop_mode == native.GL_PPR_STOP_PER_COLUMN:
+            # Every launched step wrote the next buffer (frozen columns are
+            # copied), so the final state is the last buffer written.
+            steps_run = min(done, self.max_iterations)
+            X = self.bufs[steps_run % 2]
+        else:
+            X = self.bufs[iterations % 2]
+        return PprResult(X=X, iterations=iterations, converged=converged, history=history,
+                         column_iterations=col_iter)

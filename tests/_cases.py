@@ -1,0 +1,53 @@
+"""Shared input generators and comparison helpers for the tests."""
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+import scipy.sparse as sp
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+PBR_KEYS = ["block_codes", "block_coords", "block_offsets", "block_data",
+            "remainder_indptr", "remainder_col_ind", "remainder_data"]
+
+
+def random_csr(n, density, dtype=np.float32, seed=42, m=None):
+    """The reference tests' generator (``Tests/test_spmm.py:13-15``)."""
+    return sp.random(n, n if m is None else m, density=density, format="csr", dtype=dtype,
+                     random_state=np.random.default_rng(seed).integers(2**31))
+
+
+def random_x(n, f, seed=0):
+    """``Tests/test_spmm.py:18-19``."""
+    return np.random.default_rng(seed).random((n, f)).astype(np.float32)
+
+
+def load_builder_cases():
+    z = np.load(GOLDEN / "builder_cases.npz")
+    out = []
+    for name in z["names"]:
+        name = str(name)
+        rows, cols, br, bc, mn, tot = (int(x) for x in z[f"{name}/meta"])
+        A = sp.csr_matrix((z[f"{name}/data"], z[f"{name}/indices"], z[f"{name}/indptr"]),
+                          shape=(rows, cols))
+        ref = {k: z[f"{name}/{k}"] for k in PBR_KEYS}
+        ref["total_nnz"] = tot
+        out.append((name, A, br, bc, mn, ref))
+    return out
+
+
+def assert_pbr_equal(got: dict, want: dict, ctx: str = ""):
+    """Bit-exact comparison of PBR arrays (values compared as raw bytes)."""
+    for k in PBR_KEYS:
+        a = np.asarray(got[k])
+        b = np.asarray(want[k])
+        assert a.shape == b.shape, f"{ctx} {k}: shape {a.shape} != {b.shape}"
+        if a.dtype != b.dtype:
+            assert a.dtype.kind == b.dtype.kind and a.itemsize == b.itemsize or \
+                np.array_equal(a.astype(np.int64), b.astype(np.int64)), f"{ctx} {k}: dtype {a.dtype} vs {b.dtype}"
+        if a.dtype.kind == "f":
+            assert a.dtype == b.dtype, f"{ctx} {k}: dtype {a.dtype} vs {b.dtype}"
+            assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), f"{ctx} {k}: values differ"
+        else:
+            assert np.array_equal(a.astype(np.uint64) if k == "block_codes" else a,
+                                  b.astype(np.uint64) if k == "block_codes" else b), f"{ctx} {k}: differ"

@@ -1,0 +1,42 @@
+"""The C-ABI library builds, loads, and exports every function the public
+header declares.  No compute call is made (CPU machines have no GPU)."""
+import re
+from pathlib import Path
+
+from page_rank_gb300 import native
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "graph_link_gb300.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\*?\s*(gl_[a-z0-9_]+)\s*\(", text, re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_functions():
+    names = declared_functions()
+    assert "gl_pbr_spmm" in names and "gl_ppr_step" in names and "gl_pbr_build_fill" in names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = native.lib()
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_bindings_cover_header():
+    assert sorted(native.exported_symbols()) == declared_functions()
+
+
+def test_version_and_error_text():
+    lib = native.lib()
+    assert lib.gl_version() >= 100
+    assert isinstance(lib.gl_last_error(), bytes)
+
+
+def test_workspace_query_is_host_only():
+    lib = native.lib()
+    assert lib.gl_pbr_build_workspace_bytes(1000, 1000, 5000, 8, 8) > 0
+    assert lib.gl_pbr_build_workspace_bytes(-1, 10, 10, 2, 2) < 0

@@ -1,0 +1,103 @@
+"""GPU builder parity: bit-exact against the oracle (and the reference's
+golden output), including the order of blocks inside each stripe."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import oracle
+from tests._cases import PBR_KEYS, assert_pbr_equal, load_builder_cases
+
+pytestmark = pytest.mark.gpu
+
+CASES = load_builder_cases()
+
+
+def _gpu(A, br, bc, mn):
+    from page_rank_gb300 import graph_link as gl
+    p = gl.csr_to_pbr(A, block_rows=br, block_cols=bc, min_nnz_per_block=mn)
+    d = {k: getattr(p, k) for k in PBR_KEYS}
+    d["total_nnz"] = p.total_nnz
+    return p, d
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_builder_matches_reference_golden(case, device):
+    name, A, br, bc, mn, ref = case
+    p, got = _gpu(A, br, bc, mn)
+    assert got["total_nnz"] == ref["total_nnz"]
+    assert_pbr_equal(got, ref, name)
+    expect_cls = {(np.dtype(np.int32), np.dtype(np.float32)): "PBRMatrixInt32Float",
+                  (np.dtype(np.int64), np.dtype(np.float32)): "PBRMatrixInt64Float",
+                  (np.dtype(np.int32), np.dtype(np.float64)): "PBRMatrixInt32Double",
+                  (np.dtype(np.int64), np.dtype(np.float64)): "PBRMatrixInt64Double"}
+    assert type(p).__name__ == expect_cls[(A.indices.dtype, A.data.dtype)]
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_builder_random_vs_oracle(seed, device):
+    rng = np.random.default_rng(1000 + seed)
+    for _ in range(10):
+        n = int(rng.integers(1, 2000))
+        m = int(rng.integers(1, 2000))
+        dens = float(rng.choice([0.002, 0.01, 0.05, 0.2]))
+        A = sp.random(n, m, density=dens, format="csr", dtype=np.float32,
+                      random_state=int(rng.integers(1 << 30)))
+        br = int(rng.choice([1, 2, 3, 4, 8]))
+        bc = br if rng.random() < 0.7 else int(rng.choice([1, 2, 4, 8]))
+        mn = int(rng.integers(0, 12))
+        if rng.random() < 0.25:
+            A = A.astype(np.float64)
+        if rng.random() < 0.25:
+            A = sp.csr_matrix((A.data, A.indices.astype(np.int64), A.indptr.astype(np.int64)), shape=A.shape)
+        want = oracle.csr_to_pbr(A.indptr, A.indices, A.data, n, m, br, bc, mn)
+        _, got = _gpu(A, br, bc, mn)
+        assert_pbr_equal(got, want, f"n={n} m={m} b={br}x{bc} min={mn}")
+
+
+def test_builder_int32_key_truncation(device):
+    n = 150000
+    r = np.random.default_rng(5)
+    k = 300000
+    A = sp.csr_matrix((r.random(k).astype(np.float32), (r.integers(0, n, k), r.integers(0, n, k))),
+                      shape=(n, n))
+    for br, mn in ((2, 1), (4, 2)):
+        want = oracle.csr_to_pbr(A.indptr, A.indices, A.data, n, n, br, br, mn)
+        _, got = _gpu(A, br, br, mn)
+        assert_pbr_equal(got, want, f"truncation b={br}")
+
+
+def test_builder_rehash_within_and_across_stripes(device):
+    """Stripes with many distinct blocks (the map grows mid-stripe) followed
+    by small ones (it keeps its buckets)."""
+    rng = np.random.default_rng(9)
+    dense = sp.random(24, 20000, density=0.3, format="csr", dtype=np.float32, random_state=1)
+    sparse = sp.random(200, 20000, density=0.001, format="csr", dtype=np.float32, random_state=2)
+    A = sp.vstack([sparse, dense, sparse]).tocsr()
+    for br in (2, 8):
+        want = oracle.csr_to_pbr(A.indptr, A.indices, A.data, A.shape[0], A.shape[1], br, br, 1)
+        _, got = _gpu(A, br, br, 1)
+        assert_pbr_equal(got, want, f"rehash b={br}")
+
+
+def test_builder_rejects_bad_input(device):
+    from page_rank_gb300 import graph_link as gl
+    A = sp.random(16, 16, density=0.3, format="csr", dtype=np.float32, random_state=0)
+    with pytest.raises(ValueError):
+        gl.csr_to_pbr(A, block_rows=9, block_cols=9)   # 81 bits > 64
+    with pytest.raises(TypeError):
+        gl.csr_to_pbr(A, min_nnz_per_block=300)
+    with pytest.raises(TypeError):
+        gl.csr_to_pbr(A.toarray())
+
+
+def test_noncanonical_input_is_canonicalized(device):
+    from page_rank_gb300 import graph_link as gl
+    indptr = np.array([0, 3, 5, 5, 7], np.int32)
+    indices = np.array([3, 1, 0, 2, 2, 1, 0], np.int32)
+    data = np.arange(1, 8, dtype=np.float32)
+    A = sp.csr_matrix((data, indices, indptr), shape=(4, 4))
+    C = A.copy()
+    C.sum_duplicates()
+    want = oracle.csr_to_pbr(C.indptr, C.indices, C.data, 4, 4, 2, 2, 2)
+    _, got = _gpu(A, 2, 2, 2)
+    assert_pbr_equal(got, want, "canonicalized")

@@ -1,0 +1,100 @@
+"""Fused power-iteration PPR against NetworkX (golden values, the reference's
+own accuracy test) and against the FP64 oracle."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import torch
+
+from oracle import ppr as oppr
+from tests._cases import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+NX = np.load(GOLDEN / "ppr_nx_cases.npz")
+
+
+def _gl():
+    from page_rank_gb300 import graph_link
+    return graph_link
+
+
+def _nx_matrix(N):
+    k = f"N{N}"
+    return sp.csr_matrix((NX[f"{k}/data"], NX[f"{k}/indices"], NX[f"{k}/indptr"]), shape=(N, N))
+
+
+@pytest.mark.parametrize("N", [50, 100])
+@pytest.mark.parametrize("alpha", [0.85, 0.90])
+@pytest.mark.parametrize("block_size", [2, 4, 8])
+@pytest.mark.parametrize("min_nnz", [1, 4])
+def test_ppr_accuracy_vs_networkx(N, alpha, block_size, min_nnz, device):
+    """Tests/test_ppr_accuracy.py:58-96 with the NetworkX values as fixtures."""
+    A = _nx_matrix(N)
+    sources = [0, N // 4, N // 2, N - 1]
+    pbr = _gl().csr_to_pbr(A, block_rows=block_size, block_cols=block_size,
+                           min_nnz_per_block=min_nnz).to(device)
+    X, _, converged = _gl().run_personalized_pagerank(
+        pbr, torch.tensor(sources, dtype=torch.int32, device=device), alpha=alpha,
+        max_iterations=500, tolerance=1e-6)
+    assert converged
+    X = X.cpu().numpy()
+    for k, src in enumerate(sources):
+        col = X[:, k]
+        ref = NX[f"N{N}/a{alpha}/s{src}"]
+        assert np.isclose(col.sum(), 1.0, atol=1e-4)
+        assert np.allclose(col, ref, atol=1e-3)
+
+
+@pytest.mark.parametrize("block_size", [2, 4, 8])
+def test_ppr_matches_fp64_power_iteration(block_size, device):
+    """Same update and stop rule as the reference loop: same iteration count,
+    and the FP32 result within 1e-6 L1 per column of the FP64 iterate."""
+    A = _nx_matrix(100)
+    sources = [3, 17, 42, 99, 0]
+    V = oppr.teleport_matrix(100, [[s] for s in sources])
+    X64, it64, conv64, hist64 = oppr.power_iteration_fp64(A, V, 0.85, 200, 1e-6)
+    pbr = _gl().csr_to_pbr(A, block_size, block_size, 2).to(device)
+    X, it, conv, hist = _gl().run_personalized_pagerank(
+        pbr, torch.tensor(sources, dtype=torch.int32, device=device), alpha=0.85,
+        max_iterations=200, tolerance=1e-6, return_history=True)
+    assert conv and conv64
+    assert abs(it - it64) <= 1
+    assert len(hist) == it
+    l1 = np.abs(X.cpu().numpy().astype(np.float64) - X64).sum(axis=0)
+    assert l1.max() <= 1e-6, l1
+
+
+def test_ppr_not_converged_and_zero_iterations(device):
+    gl = _gl()
+    A = _nx_matrix(50)
+    pbr = gl.csr_to_pbr(A, 4, 4, 1).to(device)
+    src = torch.tensor([1, 2], dtype=torch.int32, device=device)
+    X, it, conv, hist = gl.run_personalized_pagerank(pbr, src, max_iterations=3, tolerance=1e-12,
+                                                     return_history=True)
+    assert it == 3 and not conv and len(hist) == 3
+    X0, it0, conv0 = gl.run_personalized_pagerank(pbr, src, max_iterations=0)
+    assert it0 == 0 and not conv0
+    e = np.zeros((50, 2), np.float32)
+    e[1, 0] = e[2, 1] = 1.0
+    assert np.array_equal(X0.cpu().numpy(), e)
+
+
+def test_ppr_int64_sources_and_bad_source(device):
+    gl = _gl()
+    pbr = gl.csr_to_pbr(_nx_matrix(50), 2, 2, 1).to(device)
+    X, it, conv = gl.run_personalized_pagerank(pbr, torch.tensor([0, 5], device=device))
+    assert conv
+    with pytest.raises(ValueError):
+        gl.run_personalized_pagerank(pbr, torch.tensor([50], dtype=torch.int32, device=device))
+
+
+def test_ppr_float64_matrix(device):
+    gl = _gl()
+    A = _nx_matrix(50).astype(np.float64)
+    pbr = gl.csr_to_pbr(A, 4, 4, 1).to(device)
+    X, it, conv = gl.run_personalized_pagerank(pbr, torch.tensor([7], dtype=torch.int32, device=device),
+                                               tolerance=1e-10, max_iterations=500)
+    assert X.dtype == torch.float64 and conv
+    V = oppr.teleport_matrix(50, [[7]])
+    X64 = oppr.direct_solve_fp64(A, V, 0.85)
+    assert np.abs(X.cpu().numpy() - X64).sum() < 1e-8

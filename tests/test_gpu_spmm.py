@@ -1,0 +1,156 @@
+"""Fused PBR + CSR-remainder SpMM against the FP64 oracle.
+
+Mirrors the reference grid (Tests/test_spmm.py:37-88: atol 1e-4) and adds the
+relative bound Y vs scipy FP64 <= 1e-5 (nonnegative inputs, so no
+cancellation), 3-D batches, FP64 matrices and empty edge cases."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import torch
+
+from oracle.spmm import spmm_csr_fp64
+from tests._cases import random_csr, random_x
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-5
+
+
+def _gl():
+    from page_rank_gb300 import graph_link
+    return graph_link
+
+
+def _check(Y, Yref):
+    Y = np.asarray(Y, dtype=np.float64)
+    assert Y.shape == Yref.shape
+    assert np.allclose(Y, Yref, atol=1e-4), f"max abs diff {np.abs(Y - Yref).max():.3e}"
+    scale = np.maximum(np.abs(Yref), 1e-30)
+    rel = (np.abs(Y - Yref) / scale)[np.abs(Yref) > 1e-30]
+    assert rel.size == 0 or rel.max() <= REL_TOL, f"max rel err {rel.max():.3e}"
+
+
+@pytest.mark.parametrize("N", [64, 128, 1024])
+@pytest.mark.parametrize("num_features", [8, 64, 256])
+@pytest.mark.parametrize("density", [0.05, 0.15])
+@pytest.mark.parametrize("block_size", [2, 4, 8])
+@pytest.mark.parametrize("min_nnz", [1, 4])
+def test_spmm_accuracy(N, num_features, density, block_size, min_nnz, device):
+    A = random_csr(N, density)
+    X = random_x(N, num_features)
+    pbr = _gl().csr_to_pbr(A, block_rows=block_size, block_cols=block_size,
+                           min_nnz_per_block=min_nnz).to(device)
+    Y = _gl().pbr_matmul(pbr, torch.from_numpy(X).to(device)).cpu().numpy()
+    _check(Y, spmm_csr_fp64(A, X))
+
+
+@pytest.mark.parametrize("num_features", [1, 2, 3, 5, 6, 7, 9, 12, 17, 33, 65, 130])
+@pytest.mark.parametrize("block_size", [2, 4, 8])
+@pytest.mark.parametrize("min_nnz", [1, 4])
+def test_spmm_odd_feature_counts(num_features, block_size, min_nnz, device):
+    A = random_csr(128, 0.1)
+    X = random_x(128, num_features)
+    pbr = _gl().csr_to_pbr(A, block_rows=block_size, block_cols=block_size,
+                           min_nnz_per_block=min_nnz).to(device)
+    Y = _gl().pbr_matmul(pbr, torch.from_numpy(X).to(device)).cpu().numpy()
+    _check(Y, spmm_csr_fp64(A, X))
+
+
+@pytest.mark.parametrize("block_size", [2, 4, 8])
+def test_spmm_batched_3d_and_ragged_rows(block_size, device):
+    A = random_csr(203, 0.08, m=203)
+    rng = np.random.default_rng(3)
+    X = rng.random((3, 203, 40)).astype(np.float32)
+    pbr = _gl().csr_to_pbr(A, block_rows=block_size, block_cols=block_size, min_nnz_per_block=2).to(device)
+    Y = _gl().pbr_matmul(pbr, torch.from_numpy(X).to(device)).cpu().numpy()
+    _check(Y, spmm_csr_fp64(A, X))
+
+
+@pytest.mark.parametrize("F", [1, 20, 64, 100])
+def test_spmm_float64(F, device):
+    A = random_csr(300, 0.05, dtype=np.float64)
+    X = np.random.default_rng(1).random((300, F))
+    pbr = _gl().csr_to_pbr(A, block_rows=4, block_cols=4, min_nnz_per_block=2).to(device)
+    Y = _gl().pbr_matmul(pbr, torch.from_numpy(X).to(device)).cpu().numpy()
+    assert np.allclose(Y, spmm_csr_fp64(A, X), rtol=1e-12, atol=1e-12)
+
+
+def test_spmm_rectangular(device):
+    A = random_csr(96, 0.1, m=160)
+    X = random_x(160, 64)
+    pbr = _gl().csr_to_pbr(A, block_rows=8, block_cols=8, min_nnz_per_block=3).to(device)
+    Y = _gl().pbr_matmul(pbr, torch.from_numpy(X).to(device)).cpu().numpy()
+    _check(Y, spmm_csr_fp64(A, X))
+
+
+def test_spmm_empty_matrix_and_all_remainder(device):
+    gl = _gl()
+    A = sp.csr_matrix((64, 64), dtype=np.float32)
+    pbr = gl.csr_to_pbr(A, 4, 4, 1).to(device)
+    X = torch.rand(64, 16, device=device)
+    assert torch.count_nonzero(gl.pbr_matmul(pbr, X)) == 0
+    B = random_csr(64, 0.1)
+    pbr = gl.csr_to_pbr(B, 8, 8, 65).to(device)    # nothing packs: all remainder
+    assert pbr.accounted_blocks() == 0
+    Xn = random_x(64, 16)
+    _check(gl.pbr_matmul(pbr, torch.from_numpy(Xn).to(device)).cpu().numpy(), spmm_csr_fp64(B, Xn))
+
+
+def test_spmm_reference_uploaded_arrays(device):
+    """A matrix whose arrays came from elsewhere (the oracle builder, standing
+    in for the reference's host builder) works after the stripe index is
+    derived on the device."""
+    import oracle
+    from page_rank_gb300 import pbr as pbrmod
+    from page_rank_gb300 import native
+    A = random_csr(256, 0.05)
+    o = oracle.csr_to_pbr(A.indptr, A.indices, A.data, 256, 256, 4, 4, 2)
+    meta = {
+        "codes": torch.from_numpy(o["block_codes"].view(np.int64)).to(device),
+        "coords": torch.from_numpy(o["block_coords"]).to(device),
+        "offsets": torch.from_numpy(o["block_offsets"]).to(device),
+        "data": torch.from_numpy(o["block_data"]).to(device),
+        "rem_indptr": torch.from_numpy(o["remainder_indptr"]).to(device),
+        "rem_col_ind": torch.from_numpy(o["remainder_col_ind"]).to(device),
+        "rem_vals": torch.from_numpy(o["remainder_data"]).to(device),
+    }
+    meta["stripe_ptr"] = pbrmod.stripe_index(meta["coords"], 256, 4)
+    X = random_x(256, 32)
+    Xt = torch.from_numpy(X).to(device)
+    Y = torch.empty(256, 32, device=device)
+    desc = pbrmod.matrix_desc(meta, 256, 256, 4, 4)
+    native.check(native.lib().gl_pbr_spmm(desc, Xt.data_ptr(), Y.data_ptr(), 1, 32,
+                                          torch.cuda.current_stream().cuda_stream))
+    _check(Y.cpu().numpy(), spmm_csr_fp64(A, X))
+
+
+def test_spmm_unsupported_block_and_errors(device):
+    gl = _gl()
+    A = random_csr(64, 0.1)
+    pbr = gl.csr_to_pbr(A, block_rows=3, block_cols=3, min_nnz_per_block=1).to(device)
+    with pytest.raises(ValueError, match="Only 2x2, 4x4, and 8x8"):
+        gl.pbr_matmul(pbr, torch.rand(64, 4, device=device))
+    pbr_host = gl.csr_to_pbr(A, 2, 2, 1)
+    with pytest.raises(RuntimeError, match="not on GPU"):
+        gl.pbr_batched_matmul_cuda(pbr_host, torch.rand(64, 4, device=device))
+    with pytest.raises(TypeError):
+        gl.pbr_matmul(pbr_host, torch.rand(64, 4))
+    with pytest.raises(ValueError):
+        gl.pbr_matmul(pbr_host.to(device), torch.rand(63, 4, device=device))
+
+
+def test_to_semantics(device):
+    gl = _gl()
+    A = random_csr(64, 0.1)
+    p = gl.csr_to_pbr(A)
+    assert gl.get_pbr_gpu_meta(p) is None
+    q = p.to("cuda")
+    assert q is not p and gl.get_pbr_gpu_meta(q) is not None
+    # the reference compares str(torch.device(...)): "cuda:0" matches the
+    # tensors' device, bare "cuda" does not and yields a fresh copy
+    assert q.to("cuda:0") is q
+    assert q.to("cuda") is not q
+    c = q.to("cpu")
+    assert gl.get_pbr_gpu_meta(c) is None
+    gl.clear_pbr_gpu_meta(q)
+    assert gl.get_pbr_gpu_meta(q) is None
