@@ -1,0 +1,432 @@
+"""Benchmark: fused PBR + CSR-remainder SpMM on the 2**20-node clustered R-MAT graph.
+
+Workload (one "step" = one SpMM of the whole matrix with one dense block):
+  n = 2**20 nodes in 16384 clusters of 64, mean out-degree 16, 70% of edges
+  to a uniform in-cluster target, 30% R-MAT (0.57, 0.19, 0.19, 0.05),
+  values 1/out-degree (FP32); X ~ U[0,1) with 64 FP32 columns; PBR 8x8 blocks
+  with min_nnz_per_block = 8 plus the CSR remainder.  Seeded synthetic data
+  (no dataset is part of the reference).
+
+Metric: algorithmic HBM bytes of one SpMM / time, in GB/s:
+  B = 20 * blocks + 4 * packed + 4 * (n + 1) + 8 * remainder + 4 * n * F (X)
+      + 4 * n * F (Y)
+(code 8 + coords 8 + offset 4 per block; value 4 per packed entry; remainder
+indptr 4 per row, column 4 + value 4 per entry; X read once, Y written once).
+
+Usage:
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU
+(the path has no exchange step); rank 0 prints the JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "SpMM HBM GB/s (frac of peak)"
+UNIT = "GB/s"
+WORKLOAD = ("spmm: n=2^20 clustered R-MAT (16384 clusters of 64, out-degree 16, 70% intra, "
+            "30% R-MAT .57/.19/.19/.05), X 64 FP32 columns, PBR 8x8 min_nnz 8 + CSR remainder")
+FALLBACK_HBM_GBS = 6800.0
+
+
+# ---------------------------------------------------------------------------
+def alg_bytes(nb: int, packed: int, rem: int, n: int, F: int, elem: int = 4) -> int:
+    return 20 * nb + elem * packed + 4 * (n + 1) + (4 + elem) * rem + 2 * elem * n * F
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.is_file():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic(nb_scale_bytes: int):
+    """DRAM bytes per launch from the committed ncu summary of this workload."""
+    p = ROOT / "profiles" / "spmm_stripe_kernel_rmat2e20_f64.md"
+    if not p.is_file():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return int(float(line.split(":", 1)[1].strip()))
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int, period_ms: int = 20):
+        self.gpu_index = gpu_index
+        self.period_ms = period_ms
+        self.proc = None
+        self.lines: list[tuple[float, str]] = []
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu_index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+        t0 = time.time()
+        while not self.lines and time.time() - t0 < 5.0:
+            time.sleep(0.01)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append((time.time(), line.strip()))
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, t0: float, t1: float):
+        rows = [l for (t, l) in self.lines if t0 <= t <= t1 + 0.05]
+        if not rows:
+            rows = [l for (_, l) in self.lines[-3:]]
+        mhz, max_mhz, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            parts = [x.strip() for x in r.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                mhz.append(float(parts[1]))
+                max_mhz = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not mhz:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        return {"sm_mhz": statistics.median(mhz), "sm_max_mhz": max_mhz, "reasons": sorted(reasons),
+                "samples": len(mhz)}
+
+
+# ---------------------------------------------------------------------------
+def build_workload(device, log2n: int = 20):
+    from page_rank_gb300 import synth
+
+    g = synth.cluster_rmat_graph(log2n=log2n, cluster=64, mean_degree=16, p_intra=0.7, seed=2, device=device)
+    return g
+
+
+def cpu_spmm_rate(A, X, total_bytes: int, budget_s: float = 10.0, max_reps: int = 50):
+    """Single-core FP32 scipy CSR SpMM (the reference's CPU check,
+    Tests/test_spmm.py:46), repeated on the full matrix for ~budget_s."""
+    from oracle.spmm import spmm_csr_fp32
+
+    spmm_csr_fp32(A, X)  # warm
+    reps, t0 = 0, time.perf_counter()
+    while reps < max_reps:
+        spmm_csr_fp32(A, X)
+        reps += 1
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    dt = (time.perf_counter() - t0) / reps
+    return total_bytes / dt / 1e9, reps, dt
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+
+    from page_rank_gb300 import graph_link as gl
+    from page_rank_gb300 import native
+    from page_rank_gb300.pbr import matrix_desc, spmm_workspace
+
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    native.lib()
+    g = build_workload(dev, args.log2n)
+    A = g.A
+    n, F = A.shape[0], 64
+    t_b0 = time.perf_counter()
+    pbr = gl.csr_to_pbr(A, block_rows=8, block_cols=8, min_nnz_per_block=8)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t_b0
+    pd = pbr.to(dev)
+    meta = gl.get_pbr_gpu_meta(pd)
+    nb, packed, rem = pd.accounted_blocks(), pd.compressed_nnz(), pd.remainder_nnz()
+    B = alg_bytes(nb, packed, rem, n, F)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1234 + rank)
+    X = torch.rand((n, F), generator=gen, device=dev, dtype=torch.float32)
+    Y = torch.empty((n, F), device=dev, dtype=torch.float32)
+    desc = matrix_desc(meta, n, n, 8, 8)
+    L = native.lib()
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    ws = spmm_workspace(meta, desc, 1, F, dev)
+    ws_ptr, ws_bytes = (ws.data_ptr(), ws.numel()) if ws is not None else (None, 0)
+    del g
+    torch.cuda.empty_cache()
+
+    def step():
+        native.check(L.gl_pbr_spmm(desc, X.data_ptr(), Y.data_ptr(), 1, F, ws_ptr, ws_bytes, sh))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    t0 = time.time()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t1 = time.time()
+    if world > 1:
+        dist.barrier()
+    sampler.stop()
+    ms = ev0.elapsed_time(ev1)
+    ms_t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms_max = float(ms_t.item())
+    ms_per_step = ms_max / args.steps
+    value = world * B * args.steps / (ms_max / 1e3) / 1e9
+    kernel_gbs = B / (ms / args.steps / 1e3) / 1e9
+
+    # ---- end to end through the public API with host buffers ---------------
+    x_host = torch.empty((n, F), dtype=torch.float32, pin_memory=True)
+    x_host.copy_(X.cpu())
+    y_host = torch.empty((n, F), dtype=torch.float32, pin_memory=True)
+    x_dev = torch.empty_like(X)
+
+    def e2e_step():
+        x_dev.copy_(x_host, non_blocking=True)
+        y = gl.pbr_matmul(pd, x_dev)
+        y_host.copy_(y, non_blocking=True)
+
+    for _ in range(3):
+        e2e_step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.e2e_steps
+    e2e_t = torch.tensor([e2e_ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+    e2e_value = world * B / (float(e2e_t.item()) / 1e3) / 1e9
+    # parity spot check of the last e2e result against X @ A on the device
+    clocks = sampler.summary(t0, t1)
+
+    out = None
+    if rank == 0:
+        peak, peak_kind = measured_peak()
+        traffic = profile_traffic(B)
+        out = {
+            "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 5),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded clustered R-MAT graph, X ~ U[0,1))",
+            "config": {"workload": WORKLOAD, "n": n, "features": F, "nnz": int(A.nnz),
+                       "blocks": nb, "packed_nnz": packed, "remainder_nnz": rem,
+                       "alg_bytes_per_step": B,
+                       "l2": "inputs larger than L2: %.0f MB touched per step vs 129 MB L2" % (B / 1e6),
+                       "parallelism": f"replicas x{world}", "gpu_build_s": round(build_s, 3)},
+            "roofline": {"bound": "hbm", "achieved": round(kernel_gbs, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(kernel_gbs / peak, 4), "peak_source": peak_kind,
+                         "traffic": traffic,
+                         "kernel": "stripe_kernel<float,8,8,V=2,C=32> (gl_pbr_spmm)",
+                         "heavy_pieces": int(desc.num_pieces), "heavy_stripes": int(desc.num_heavy)},
+            "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "ms_per_step": round(e2e_ms, 4),
+                    "h2d_bytes_per_step": int(x_host.numel() * 4),
+                    "d2h_bytes_per_step": int(y_host.numel() * 4),
+                    "api": "page_rank_gb300.graph_link.pbr_matmul (pinned host X -> device -> host Y)"},
+            "gpu_launches": args.steps,
+            "clocks": clocks,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            Xn = X.cpu().numpy()
+            gbs, reps, dt = cpu_spmm_rate(A, Xn, B, budget_s=args.cpu_budget)
+            out["cpu_baseline"] = {"value": round(gbs, 3), "unit": UNIT, "cores": 1, "kind": "port",
+                                   "sample": f"full SpMM (scipy FP32 CSR @ X, the reference's CPU "
+                                             f"check), {reps} reps, {dt * 1e3:.1f} ms each"}
+    return out
+
+
+# ---------------------------------------------------------------------------
+def _ref_worker(args):
+    """One row range of the CPU SpMM (runs in a spawned process)."""
+    from multiprocessing import shared_memory
+
+    import scipy.sparse as sp
+
+    names, shapes, dtypes, r0, r1, n, F, reps = args
+    shms = [shared_memory.SharedMemory(name=nm) for nm in names]
+    arrs = [np.ndarray(s, dtype=d, buffer=m.buf) for m, s, d in zip(shms, shapes, dtypes)]
+    indptr, indices, data, X, Y = arrs
+    lo, hi = int(indptr[r0]), int(indptr[r1])
+    sub = sp.csr_matrix((data[lo:hi], indices[lo:hi], indptr[r0:r1 + 1] - lo), shape=(r1 - r0, n))
+    for _ in range(reps):
+        Y[r0:r1] = sub @ X
+    for m in shms:
+        m.close()
+    return r1 - r0
+
+
+def run_reference(args, rank, world):
+    """CPU SpMM of the same workload on all host cores (the reference's CPU
+    path: FP32 scipy CSR @ X, the check in Tests/test_spmm.py:46), row-split
+    over a spawned process pool.  Each step is a bounded row sample so the
+    whole run stays within a few minutes."""
+    if rank != 0:
+        return None
+    import multiprocessing as mp
+    from multiprocessing import shared_memory
+
+    g = build_workload(None, args.log2n)
+    A = g.A
+    n, F = A.shape[0], 64
+    X = np.random.default_rng(1234).random((n, F), dtype=np.float32)
+    cores = os.cpu_count() or 1
+    arrays = [A.indptr.astype(np.int64), A.indices, A.data, X, np.zeros((n, F), np.float32)]
+    shms, names = [], []
+    for a in arrays:
+        m = shared_memory.SharedMemory(create=True, size=max(1, a.nbytes))
+        np.ndarray(a.shape, dtype=a.dtype, buffer=m.buf)[...] = a
+        shms.append(m)
+        names.append(m.name)
+    shapes = [a.shape for a in arrays]
+    dtypes = [a.dtype for a in arrays]
+    B_full = alg_bytes(0, 0, int(A.nnz), n, F)   # CSR only: indptr + col/val per nnz + X + Y
+    ctx = mp.get_context("spawn")
+    try:
+        with ctx.Pool(cores) as pool:
+            def run_rows(frac, reps):
+                rows = max(cores, int(n * frac))
+                bounds = np.linspace(0, rows, cores + 1).astype(int)
+                jobs = [(names, shapes, dtypes, int(bounds[i]), int(bounds[i + 1]), n, F, reps)
+                        for i in range(cores) if bounds[i + 1] > bounds[i]]
+                t0 = time.perf_counter()
+                pool.map(_ref_worker, jobs)
+                return time.perf_counter() - t0, rows
+            run_rows(0.05, 1)                           # warm the pool
+            t_full, _ = run_rows(1.0, 1)                # calibrate one full SpMM
+            budget = max(0.02, 150.0 / max(1, args.steps + args.warmup))
+            frac = min(1.0, budget / max(t_full, 1e-6))
+            for _ in range(args.warmup):
+                run_rows(frac, 1)
+            t0 = time.perf_counter()
+            rows_done = 0
+            for _ in range(args.steps):
+                _, rows = run_rows(frac, 1)
+                rows_done += rows
+            dt = time.perf_counter() - t0
+    finally:
+        for m in shms:
+            m.close()
+            m.unlink()
+    frac_eff = rows_done / (n * args.steps)
+    value = B_full * frac_eff * args.steps / dt / 1e9
+    ms = dt / args.steps * 1e3
+    return {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded clustered R-MAT graph, X ~ U[0,1))",
+        "config": {"workload": WORKLOAD, "n": n, "features": F, "nnz": int(A.nnz),
+                   "parallelism": f"{cores} host processes"},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"rows [0, {int(n * frac_eff)}) of the matrix per step "
+                                   f"({frac_eff:.3f} of the SpMM), FP32 scipy CSR @ X, "
+                                   f"row-split over {cores} processes"},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--log2n", type=int, default=20,
+                    help="graph size (2**log2n nodes); only for small profiling runs")
+    ap.add_argument("--workload", choices=["spmm", "ppr_small", "ppr_batched"], default="spmm",
+                    help="spmm (default, the headline line) or a secondary PPR workload")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.workload != "spmm":
+        import torch
+        from page_rank_gb300 import workloads
+        dev = torch.device("cuda", local_rank)
+        torch.cuda.set_device(dev)
+        fn = getattr(workloads, args.workload)
+        out = fn(dev) if args.workload == "ppr_small" else fn(dev, log2n=args.log2n if args.log2n != 20 else 22)
+        out = {"workload": args.workload, **out}
+    elif args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        if world > 1:
+            import torch
+            import torch.distributed as dist
+            torch.cuda.set_device(local_rank)
+            dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+        out = run_ours(args, rank, world, local_rank)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+    if out is not None and rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -54,6 +54,12 @@ int gl_version(void);
  * of stripe s (blocks are stored stripe-major, as the reference builder emits
  * them), with ceil(rows / block_rows) + 1 entries.  gl_pbr_stripe_index()
  * derives it from block_coords.
+ *
+ * The load-balance schedule (no reference counterpart) is optional: with
+ * num_pieces == 0 every stripe is one work unit.  gl_pbr_schedule_build()
+ * fills it: stripes holding more than 2 * piece_work stored entries are cut
+ * into pieces of piece_work entries, processed independently and reduced in
+ * piece order.  column_tile caps the columns one warp covers (0: automatic).
  */
 typedef struct gl_pbr_matrix {
     int64_t rows, cols;
@@ -68,6 +74,12 @@ typedef struct gl_pbr_matrix {
     const int32_t* remainder_col_ind;   /* [remainder_nnz]                   */
     const void*    remainder_data;      /* [remainder_nnz]                   */
     const int32_t* stripe_block_ptr;    /* [ceil(rows/block_rows) + 1]       */
+    /* load-balance schedule (see above) */
+    int32_t num_heavy, num_pieces, piece_work, column_tile;
+    const int32_t* heavy_of;            /* [num_stripes]: heavy index or -1  */
+    const int32_t* heavy_stripe;        /* [num_heavy]                       */
+    const int32_t* heavy_first;         /* [num_heavy + 1]: first piece      */
+    const int32_t* piece_heavy;         /* [num_pieces]: owning heavy index  */
 } gl_pbr_matrix;
 
 /* ======================================================================== */
@@ -124,6 +136,15 @@ int gl_pbr_stripe_index(const int32_t* block_coords, int64_t num_blocks, int64_t
                         int32_t block_rows, int32_t* stripe_block_ptr,
                         int32_t* flag_scratch, cudaStream_t stream);
 
+/* int32 elements of the buffer gl_pbr_schedule_build() needs. */
+int64_t gl_pbr_schedule_elems(const gl_pbr_matrix* A, int32_t piece_work);
+
+/* Builds the load-balance schedule of A into `buffer` (device int32,
+ * gl_pbr_schedule_elems() entries) and sets A's schedule fields to point into
+ * it.  piece_work <= 0 selects the default (256).  Synchronizes `stream`. */
+int gl_pbr_schedule_build(gl_pbr_matrix* A, int32_t piece_work, int32_t* buffer, int64_t buffer_elems,
+                          cudaStream_t stream);
+
 /* ======================================================================== */
 /* Fused PBR-block + CSR-remainder SpMM                                     */
 /* Replaces pbr_spmm_cuda_dispatch (bindings/bindings_kernels.cu:13-83) and
@@ -134,8 +155,15 @@ int gl_pbr_stripe_index(const int32_t* block_coords, int64_t num_blocks, int64_t
 /* X: [batch][cols][features], Y: [batch][rows][features], both contiguous,
  * element type A->value_type.  Supported blocks: 2x2, 4x4, 8x8 (others give
  * GL_ERR_UNSUPPORTED_BLOCK, as the reference throws std::invalid_argument). */
+/* Workspace (bytes) of gl_pbr_spmm / gl_ppr_step for A's schedule: partial
+ * tiles of the heavy-stripe pieces plus one counter per heavy stripe and
+ * tile.  It must be zero-filled before its first use; every call leaves the
+ * counters at zero again, so it can be reused (not concurrently). */
+int64_t gl_pbr_spmm_workspace_bytes(const gl_pbr_matrix* A, int64_t batch, int64_t features);
+
 int gl_pbr_spmm(const gl_pbr_matrix* A, const void* X, void* Y,
-                int64_t batch, int64_t features, cudaStream_t stream);
+                int64_t batch, int64_t features, void* workspace, int64_t workspace_bytes,
+                cudaStream_t stream);
 
 /* ======================================================================== */
 /* Personalized PageRank                                                    */
@@ -183,6 +211,9 @@ int gl_ppr_dangling_mass(const void* X, int64_t rows, int64_t K, int32_t value_t
 #define GL_PPR_STOP_ALL        0  /* stop every column when max_k residual < tol */
 #define GL_PPR_STOP_PER_COLUMN 1  /* freeze column k once its residual < tol     */
 
+#define GL_DANGLING_TO_TELEPORT 0 /* dangling mass returns through v_k          */
+#define GL_DANGLING_UNIFORM     1 /* dangling mass spreads as 1/rows over rows   */
+
 /*
  * One fused power-iteration step (SpMM + alpha-scaling + teleport + dangling
  * mass + per-column L1 residual in one pass):
@@ -190,6 +221,12 @@ int gl_ppr_dangling_mass(const void* X, int64_t rows, int64_t K, int32_t value_t
  *   X_out[:, k] = alpha * A X_in[:, k] + ((1 - alpha) + alpha * d_t[k]) * v_k
  *   residual[t][k] = sum_i |X_out[i, k] - X_in[i, k]|
  *   d_{t+1}[k]     = sum over dangling rows i of X_out[i, k]
+ *
+ * or, with dangling_target == GL_DANGLING_UNIFORM, the dangling mass is spread
+ * evenly instead: X_out[:, k] = alpha * A X_in[:, k] + alpha * d_t[k] / rows
+ * + (1 - alpha) * v_k — the same fixed point as the reference's
+ * normalize_transition_matrix (graph_link/__init__.py:200-206), which stores a
+ * dense 1/N column per dangling node, without storing those columns.
  *
  * where v_k is the teleport vector of column k and d_t the dangling mass of
  * X_in (zero when dangling_bitmap is NULL — the column-stochastic case of the
@@ -205,6 +242,7 @@ int gl_ppr_dangling_mass(const void* X, int64_t rows, int64_t K, int32_t value_t
  * dangling_hist.  A step is a no-op when t >= max_iterations, or (STOP_ALL)
  * when max_k residual_hist[t-1][k] < tol.  Under STOP_PER_COLUMN, a column
  * whose residual_hist[t-1][k] < tol is copied unchanged and adds 0.
+ * workspace: as for gl_pbr_spmm with batch 1 and K features.
  */
 typedef struct gl_ppr_step_params {
     double  alpha;
@@ -216,11 +254,13 @@ typedef struct gl_ppr_step_params {
     double*         residual_hist;    /* device [max_iterations][K]          */
     double*         dangling_hist;    /* device [max_iterations + 1][K]      */
     const uint32_t* dangling_bitmap;  /* device, ceil(rows/32) words, or NULL */
+    int32_t         dangling_target;  /* GL_DANGLING_TO_TELEPORT / _UNIFORM  */
 } gl_ppr_step_params;
 
 int gl_ppr_step(const gl_pbr_matrix* A, const gl_teleport* tp,
                 const void* X_in, void* X_out, int64_t K,
-                const gl_ppr_step_params* params, cudaStream_t stream);
+                const gl_ppr_step_params* params, void* workspace, int64_t workspace_bytes,
+                cudaStream_t stream);
 
 /* Adds `delta` to the device int32 at `counter` (stream-ordered; the node
  * that advances chunk_base at the end of a captured chunk of steps). */

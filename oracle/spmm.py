@@ -29,3 +29,9 @@ def spmm_pbr_fp64(pbr: dict, X: np.ndarray) -> np.ndarray:
     r, c, v = expand_pbr_coo(pbr)
     A = sp.csr_matrix((v.astype(np.float64), (r, c)), shape=(pbr["rows"], pbr["cols"]))
     return spmm_csr_fp64(A, X)
+
+
+def spmm_csr_fp32(A: sp.csr_matrix, X: np.ndarray) -> np.ndarray:
+    """A @ X in float32 with scipy — the CPU SpMM the reference's own tests
+    run (``Tests/test_spmm.py:46``); used as the timed CPU baseline."""
+    return np.asarray(A @ X)

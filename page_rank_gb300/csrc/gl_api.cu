@@ -2,6 +2,7 @@
 // PageRank entry points (teleport index, init, fused step).
 #include <cstdarg>
 #include <cstdio>
+#include <vector>
 
 #include "gl_common.cuh"
 #include "gl_scan.cuh"
@@ -53,7 +54,51 @@ StripeArgs<S> make_args(const gl_pbr_matrix* A) {
     a.cols = A->cols;
     a.nstripes = ceil_div(A->rows, A->block_rows);
     a.batch = 1;
+    a.num_pieces = A->num_pieces > 0 && A->heavy_of ? A->num_pieces : 0;
+    a.piece_work = A->piece_work;
+    a.heavy_of = a.num_pieces ? A->heavy_of : nullptr;
+    a.heavy_stripe = A->heavy_stripe;
+    a.heavy_first = A->heavy_first;
+    a.piece_heavy = A->piece_heavy;
     return a;
+}
+
+inline int64_t align256(int64_t x) { return (x + 255) & ~int64_t(255); }
+
+int64_t partial_bytes(const gl_pbr_matrix* A, int64_t batch, int64_t K) {
+    if (A->num_pieces <= 0) return 0;
+    const int64_t elem = A->value_type == GL_F32 ? 4 : 8;
+    const int64_t Kt = ceil_div(K, 128) * 128;
+    return align256((int64_t)A->num_pieces * batch * A->block_rows * Kt * elem);
+}
+
+int64_t workspace_bytes(const gl_pbr_matrix* A, int64_t batch, int64_t K) {
+    if (A->num_pieces <= 0) return 0;
+    return partial_bytes(A, batch, K) + align256((int64_t)A->num_heavy * batch * K * 4);
+}
+
+// Points the kernel's partial / counter buffers into the caller's workspace.
+template <typename S>
+int bind_workspace(StripeArgs<S>& a, const gl_pbr_matrix* A, int64_t batch, int64_t K, void* ws,
+                   int64_t ws_bytes) {
+    if (a.num_pieces == 0) return GL_OK;
+    const int64_t need = workspace_bytes(A, batch, K);
+    GL_REQUIRE(ws != nullptr && ws_bytes >= need, GL_ERR_WORKSPACE,
+               "SpMM workspace of %lld bytes needed (gl_pbr_spmm_workspace_bytes)", (long long)need);
+    char* base = static_cast<char*>(ws);
+    a.partial = reinterpret_cast<S*>(base);
+    a.counters = reinterpret_cast<int32_t*>(base + partial_bytes(A, batch, K));
+    return GL_OK;
+}
+
+__global__ void stripe_work_kernel(const int32_t* stripe_ptr, const int32_t* offsets, const int32_t* rem_ptr,
+                                   int64_t rows, int br, int64_t ns, int32_t* work) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= ns) return;
+    const int64_t last = (s * br + br < rows) ? s * br + br : rows;
+    const int64_t w = (int64_t)offsets[stripe_ptr[s + 1]] - offsets[stripe_ptr[s]] +
+                      (int64_t)rem_ptr[last] - rem_ptr[s * br];
+    work[s] = (int32_t)(w < INT32_MAX ? w : INT32_MAX);
 }
 
 __global__ void stripe_index_kernel(const int32_t* coords, int64_t nb, int64_t rows, int br, int64_t ns,
@@ -141,8 +186,72 @@ using namespace gl;
 extern "C" const char* gl_last_error(void) { return last_error(); }
 extern "C" int gl_version(void) { return 100; }
 
+extern "C" int64_t gl_pbr_spmm_workspace_bytes(const gl_pbr_matrix* A, int64_t batch, int64_t features) {
+    if (A == nullptr || batch < 0 || features < 0) return -1;
+    return workspace_bytes(A, batch, features);
+}
+
+extern "C" int64_t gl_pbr_schedule_elems(const gl_pbr_matrix* A, int32_t piece_work) {
+    if (A == nullptr || A->block_rows < 1) return -1;
+    const int64_t w = piece_work > 0 ? piece_work : 256;
+    const int64_t ns = ceil_div(A->rows, A->block_rows);
+    return 4 * ns + 8 + (A->packed_nnz + A->remainder_nnz) / w;
+}
+
+extern "C" int gl_pbr_schedule_build(gl_pbr_matrix* A, int32_t piece_work, int32_t* buffer, int64_t buffer_elems,
+                                     cudaStream_t stream) {
+    GL_REQUIRE(A != nullptr && A->block_rows >= 1, GL_ERR_INVALID_ARGUMENT, "bad matrix");
+    const int32_t W = piece_work > 0 ? piece_work : 256;
+    const int64_t need = gl_pbr_schedule_elems(A, W);
+    GL_REQUIRE(buffer != nullptr && buffer_elems >= need, GL_ERR_WORKSPACE, "schedule buffer of %lld int32 needed",
+               (long long)need);
+    const int64_t ns = ceil_div(A->rows, A->block_rows);
+    A->num_heavy = 0;
+    A->num_pieces = 0;
+    A->piece_work = W;
+    A->heavy_of = nullptr;
+    if (ns == 0) return GL_OK;
+    stripe_work_kernel<<<(unsigned)ceil_div(ns, 256), 256, 0, stream>>>(A->stripe_block_ptr, A->block_offsets,
+                                                                        A->remainder_indptr, A->rows, A->block_rows,
+                                                                        ns, buffer);
+    GL_LAUNCH_CHECK("stripe_work_kernel");
+    std::vector<int32_t> work(ns);
+    GL_CUDA_TRY(cudaMemcpyAsync(work.data(), buffer, sizeof(int32_t) * ns, cudaMemcpyDeviceToHost, stream));
+    GL_CUDA_TRY(cudaStreamSynchronize(stream));
+    std::vector<int32_t> heavy_of(ns, -1), heavy_stripe, heavy_first(1, 0), piece_heavy;
+    for (int64_t s = 0; s < ns; ++s) {
+        if (work[s] > 2 * W) {
+            const int32_t h = (int32_t)heavy_stripe.size();
+            const int32_t np = (int32_t)ceil_div(work[s], W);
+            heavy_of[s] = h;
+            heavy_stripe.push_back((int32_t)s);
+            for (int32_t q = 0; q < np; ++q) piece_heavy.push_back(h);
+            heavy_first.push_back((int32_t)piece_heavy.size());
+        }
+    }
+    const int64_t H = (int64_t)heavy_stripe.size(), NP = (int64_t)piece_heavy.size();
+    if (H == 0) return GL_OK;
+    GL_REQUIRE(ns + H + (H + 1) + NP <= buffer_elems, GL_ERR_WORKSPACE, "schedule buffer too small");
+    int32_t* d_heavy_of = buffer;
+    int32_t* d_heavy_stripe = d_heavy_of + ns;
+    int32_t* d_heavy_first = d_heavy_stripe + H;
+    int32_t* d_piece_heavy = d_heavy_first + H + 1;
+    GL_CUDA_TRY(cudaMemcpyAsync(d_heavy_of, heavy_of.data(), 4 * ns, cudaMemcpyHostToDevice, stream));
+    GL_CUDA_TRY(cudaMemcpyAsync(d_heavy_stripe, heavy_stripe.data(), 4 * H, cudaMemcpyHostToDevice, stream));
+    GL_CUDA_TRY(cudaMemcpyAsync(d_heavy_first, heavy_first.data(), 4 * (H + 1), cudaMemcpyHostToDevice, stream));
+    GL_CUDA_TRY(cudaMemcpyAsync(d_piece_heavy, piece_heavy.data(), 4 * NP, cudaMemcpyHostToDevice, stream));
+    GL_CUDA_TRY(cudaStreamSynchronize(stream));
+    A->num_heavy = (int32_t)H;
+    A->num_pieces = (int32_t)NP;
+    A->heavy_of = d_heavy_of;
+    A->heavy_stripe = d_heavy_stripe;
+    A->heavy_first = d_heavy_first;
+    A->piece_heavy = d_piece_heavy;
+    return GL_OK;
+}
+
 extern "C" int gl_pbr_spmm(const gl_pbr_matrix* A, const void* X, void* Y, int64_t batch, int64_t features,
-                           cudaStream_t stream) {
+                           void* workspace, int64_t workspace_bytes, cudaStream_t stream) {
     int rc = check_matrix(A);
     if (rc != GL_OK) return rc;
     GL_REQUIRE(batch >= 0 && features >= 0, GL_ERR_INVALID_ARGUMENT, "negative batch / features");
@@ -155,14 +264,16 @@ extern "C" int gl_pbr_spmm(const gl_pbr_matrix* A, const void* X, void* Y, int64
         a.K = (int32_t)features;
         a.X = static_cast<const float*>(X);
         a.Y = static_cast<float*>(Y);
-        return launch_stripe<float, false>(a, A->block_rows, A->block_cols, stream);
+        if ((rc = bind_workspace(a, A, batch, features, workspace, workspace_bytes)) != GL_OK) return rc;
+        return launch_stripe<float, false>(a, A->block_rows, A->block_cols, A->column_tile, stream);
     }
     StripeArgs<double> a = make_args<double>(A);
     a.batch = batch;
     a.K = (int32_t)features;
     a.X = static_cast<const double*>(X);
     a.Y = static_cast<double*>(Y);
-    return launch_stripe<double, false>(a, A->block_rows, A->block_cols, stream);
+    if ((rc = bind_workspace(a, A, batch, features, workspace, workspace_bytes)) != GL_OK) return rc;
+    return launch_stripe<double, false>(a, A->block_rows, A->block_cols, A->column_tile, stream);
 }
 
 extern "C" int gl_pbr_stripe_index(const int32_t* block_coords, int64_t num_blocks, int64_t rows, int32_t block_rows,
@@ -259,7 +370,8 @@ extern "C" int gl_ppr_dangling_mass(const void* X, int64_t rows, int64_t K, int3
 }
 
 extern "C" int gl_ppr_step(const gl_pbr_matrix* A, const gl_teleport* tp, const void* X_in, void* X_out, int64_t K,
-                           const gl_ppr_step_params* p, cudaStream_t stream) {
+                           const gl_ppr_step_params* p, void* workspace, int64_t workspace_bytes,
+                           cudaStream_t stream) {
     int rc = check_matrix(A);
     if (rc != GL_OK) return rc;
     GL_REQUIRE(tp != nullptr && p != nullptr, GL_ERR_INVALID_ARGUMENT, "NULL teleport / params");
@@ -270,6 +382,8 @@ extern "C" int gl_ppr_step(const gl_pbr_matrix* A, const gl_teleport* tp, const 
     GL_REQUIRE(p->stop_mode == GL_PPR_STOP_ALL || p->stop_mode == GL_PPR_STOP_PER_COLUMN, GL_ERR_INVALID_ARGUMENT,
                "bad stop_mode");
     GL_REQUIRE(X_in != X_out, GL_ERR_INVALID_ARGUMENT, "X_in and X_out must be different buffers");
+    GL_REQUIRE(p->dangling_target == GL_DANGLING_TO_TELEPORT || p->dangling_target == GL_DANGLING_UNIFORM,
+               GL_ERR_INVALID_ARGUMENT, "bad dangling_target");
     if (K == 0 || A->rows == 0) return GL_OK;
     GL_REQUIRE(tp->num_entries == 0 || tp->stripe_ptr, GL_ERR_INVALID_ARGUMENT, "teleport index missing");
 #define GL_FILL_PPR(a)                                     \
@@ -287,19 +401,22 @@ extern "C" int gl_ppr_step(const gl_pbr_matrix* A, const gl_teleport* tp, const 
     (a).chunk_base = p->chunk_base;                        \
     (a).res_hist = p->residual_hist;                       \
     (a).dang_hist = p->dangling_hist;                      \
-    (a).dbitmap = p->dangling_bitmap
+    (a).dbitmap = p->dangling_bitmap;                      \
+    (a).dang_uniform = p->dangling_target == GL_DANGLING_UNIFORM
     if (A->value_type == GL_F32) {
         StripeArgs<float> a = make_args<float>(A);
         GL_FILL_PPR(a);
         a.X = static_cast<const float*>(X_in);
         a.Y = static_cast<float*>(X_out);
-        return launch_stripe<float, true>(a, A->block_rows, A->block_cols, stream);
+        if ((rc = bind_workspace(a, A, 1, K, workspace, workspace_bytes)) != GL_OK) return rc;
+        return launch_stripe<float, true>(a, A->block_rows, A->block_cols, A->column_tile, stream);
     }
     StripeArgs<double> a = make_args<double>(A);
     GL_FILL_PPR(a);
     a.X = static_cast<const double*>(X_in);
     a.Y = static_cast<double*>(X_out);
-    return launch_stripe<double, true>(a, A->block_rows, A->block_cols, stream);
+    if ((rc = bind_workspace(a, A, 1, K, workspace, workspace_bytes)) != GL_OK) return rc;
+    return launch_stripe<double, true>(a, A->block_rows, A->block_cols, A->column_tile, stream);
 #undef GL_FILL_PPR
 }
 

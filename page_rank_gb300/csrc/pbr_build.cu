@@ -73,8 +73,10 @@ struct BuildWs {
     int32_t*  rec_ins;      // first-nonzero position, then insertion rank
     int32_t*  rec_tau;
     uint32_t* rec_bkt;
-    int32_t*  rec_g;        // bucket-run head tau, later: data offset
-    int32_t*  rec_pos;      // list position, later: output slot (-1 = dropped)
+    int32_t*  rec_g;        // bucket-run head tau, later: value offset in the stripe
+                            // (rec_tau later holds the output slot, -1 = dropped)
+    int32_t*  rec_pos;      // list position
+    int32_t*  rec_pops;     // popcount of the block code
     int64_t bytes;
 };
 
@@ -103,6 +105,7 @@ BuildWs layout_ws(void* base, int64_t rows, int64_t nnz, int32_t br) {
     w.rec_bkt = reinterpret_cast<uint32_t*>(take(4 * nr));
     w.rec_g = reinterpret_cast<int32_t*>(take(4 * nr));
     w.rec_pos = reinterpret_cast<int32_t*>(take(4 * nr));
+    w.rec_pops = reinterpret_cast<int32_t*>(take(4 * nr));
     w.bytes = off;
     return w;
 }
@@ -238,16 +241,38 @@ __device__ __forceinline__ uint32_t key_bucket(int64_t key_value, bool key32, ui
     return (uint32_t)((uint64_t)k % buckets);
 }
 
-// Orders the first `present` records (by insertion rank) as the standard
-// library's node list would under `buckets`; writes list positions to rec_pos.
+// A team is the set of threads that orders one stripe: a warp for stripes
+// with few distinct blocks, a whole 1024-thread CTA for big ones (R-MAT hub
+// rows put tens of thousands of blocks into one stripe).
+template <int TEAM>
+struct Team;
+template <>
+struct Team<32> {
+    static __device__ __forceinline__ int rank() { return threadIdx.x & 31; }
+    static __device__ __forceinline__ void sync() { __syncwarp(); }
+};
+template <>
+struct Team<1024> {
+    static __device__ __forceinline__ int rank() { return threadIdx.x; }
+    static __device__ __forceinline__ void sync() { __syncthreads(); }
+};
+
+constexpr int kSmallStripeBlocks = 64;   // warp team up to this many distinct blocks
+constexpr int kBigThreads = 1024;
+constexpr int kBigStage = 1536;          // big stripes up to this size are staged in shared memory
+
+// Orders the records with insertion rank < present as the standard library's
+// node list would under `buckets` (see the file comment); writes list
+// positions to pos.  O(m^2 / TEAM).
+template <int TEAM>
 __device__ void list_order(int64_t s, int64_t ncb, bool key32, uint64_t buckets, int m, int present,
                            const int64_t* bcol, const int32_t* ins, const int32_t* tau, uint32_t* bkt,
                            int32_t* g, int32_t* pos) {
-    const int lane = threadIdx.x & 31;
-    for (int e = lane; e < m; e += 32)
+    const int tr = Team<TEAM>::rank();
+    for (int e = tr; e < m; e += TEAM)
         if (ins[e] < present) bkt[e] = key_bucket(s * ncb + bcol[e], key32, buckets);
-    __syncwarp();
-    for (int e = lane; e < m; e += 32) {
+    Team<TEAM>::sync();
+    for (int e = tr; e < m; e += TEAM) {
         if (ins[e] >= present) continue;
         int32_t head = tau[e];
         const uint32_t be = bkt[e];
@@ -255,19 +280,132 @@ __device__ void list_order(int64_t s, int64_t ncb, bool key32, uint64_t buckets,
             if (ins[f] < present && bkt[f] == be && tau[f] < head) head = tau[f];
         g[e] = head;
     }
-    __syncwarp();
-    for (int e = lane; e < m; e += 32) {
+    Team<TEAM>::sync();
+    for (int e = tr; e < m; e += TEAM) {
         if (ins[e] >= present) continue;
         const int32_t ge = g[e], te = tau[e];
         int r = 0;
         for (int f = 0; f < m; ++f) {
             if (ins[f] >= present) continue;
             const int32_t gf = g[f];
-            if (gf > ge || (gf == ge && tau[f] > te)) ++r;
+            r += (gf > ge || (gf == ge && tau[f] > te)) ? 1 : 0;
         }
         pos[e] = r;
     }
-    __syncwarp();
+    Team<TEAM>::sync();
+}
+
+// Records the distinct blocks of stripe s in block-column order (warp 0 of
+// the team): code, block column and first CSR position relative to the
+// stripe start.
+template <typename I>
+__device__ void record_blocks(const I* indptr, const I* indices, int64_t s, int64_t rows, int64_t cols, int64_t nnz,
+                              int br, int bc, uint64_t* code_r, int64_t* bcol_r, int32_t* first_r) {
+    const int lane = threadIdx.x & 31;
+    StripeMerge<I> mg;
+    mg.init(indptr, indices, s, rows, nnz, br, bc, false);
+    int64_t bcol, first, my_first;
+    uint64_t code;
+    int my_count;
+    int j = 0;
+    const int64_t base = (int64_t)indptr[s * br];
+    while (mg.step(cols, bcol, code, first, my_count, my_first)) {
+        if (lane == 0) {
+            code_r[j] = code;
+            bcol_r[j] = bcol;
+            first_r[j] = (int32_t)(first - base);
+        }
+        ++j;
+    }
+}
+
+// Moves the stripe's values into block_data / the remainder (warp 0):
+// slot[j] >= 0 is the output slot of kept block j, doff[j] its value offset.
+template <typename I, typename S>
+__device__ void move_values(const I* indptr, const I* indices, const S* values, int64_t s, int64_t rows,
+                            int64_t cols, int64_t nnz, int br, int bc, const int32_t* slot, const int32_t* doff,
+                            int64_t packed_base, const int64_t* row_rem, S* out_data, I* out_rem_col,
+                            S* out_rem_val) {
+    const int lane = threadIdx.x & 31;
+    StripeMerge<I> mg;
+    mg.init(indptr, indices, s, rows, nnz, br, bc, false);
+    const int64_t row = s * br + lane;
+    int64_t rem_cursor = (lane < br && row < rows) ? row_rem[row] : 0;
+    int64_t bcol, first, my_first;
+    uint64_t code;
+    int my_count;
+    int j = 0;
+    while (mg.step(cols, bcol, code, first, my_count, my_first)) {
+        if (slot[j] >= 0) {
+            const int before = (int)warp_incl_scan_i64(my_count) - my_count;
+            const int64_t dst = packed_base + doff[j] + before;
+            for (int i = 0; i < my_count; ++i) out_data[dst + i] = values[my_first + i];
+        } else {
+            for (int i = 0; i < my_count; ++i) {
+                out_rem_col[rem_cursor + i] = indices[my_first + i];
+                out_rem_val[rem_cursor + i] = values[my_first + i];
+            }
+            rem_cursor += my_count;
+        }
+        ++j;
+    }
+}
+
+// Emit order and outputs of one stripe's m recorded blocks (team-parallel).
+// ins holds first CSR positions on entry.  slot / doff receive, per record,
+// the output slot (-1: dropped) and the value offset inside the stripe.
+template <int TEAM, typename I>
+__device__ void order_stripe(int64_t s, int m, int br, int bc, int min_nnz, int64_t ncb, bool key32, int nchain,
+                             const int64_t* chain, int64_t prefmax, int64_t kept_base, int64_t packed_base,
+                             const uint64_t* code_r, const int64_t* bcol_r, int32_t* ins, int32_t* tau,
+                             uint32_t* bkt, int32_t* g, int32_t* pos, int32_t* pops, uint64_t* out_codes,
+                             I* out_coords, I* out_offsets) {
+    const int tr = Team<TEAM>::rank();
+    for (int e = tr; e < m; e += TEAM) pops[e] = __popcll(code_r[e]);
+    // insertion rank = rank of the first CSR position
+    for (int e = tr; e < m; e += TEAM) {
+        const int32_t fe = ins[e];
+        int r = 0;
+        for (int f = 0; f < m; ++f) r += ins[f] < fe ? 1 : 0;
+        tau[e] = r;
+    }
+    Team<TEAM>::sync();
+    for (int e = tr; e < m; e += TEAM) ins[e] = tau[e];
+    Team<TEAM>::sync();
+    // bucket count at stripe start, then the rehashes inside the stripe
+    int J = 0;
+    while (J + 1 < nchain && chain[2 * (J + 1)] <= prefmax) ++J;
+    while (J + 1 < nchain && chain[2 * (J + 1)] <= m) {
+        const int present = (int)(chain[2 * (J + 1)] - 1);
+        list_order<TEAM>(s, ncb, key32, (uint64_t)chain[2 * J + 1], m, present, bcol_r, ins, tau, bkt, g, pos);
+        for (int e = tr; e < m; e += TEAM)
+            if (ins[e] < present) tau[e] = pos[e];
+        Team<TEAM>::sync();
+        ++J;
+    }
+    list_order<TEAM>(s, ncb, key32, (uint64_t)chain[2 * J + 1], m, m, bcol_r, ins, tau, bkt, g, pos);
+    // output slot and value offset of each kept block, in list order
+    for (int e = tr; e < m; e += TEAM) {
+        int slot = -1, doff = 0;
+        if (pops[e] >= min_nnz) {
+            slot = 0;
+            const int32_t pe = pos[e];
+            for (int f = 0; f < m; ++f) {
+                if (pops[f] >= min_nnz && pos[f] < pe) {
+                    ++slot;
+                    doff += pops[f];
+                }
+            }
+            const int64_t ob = kept_base + slot;
+            out_codes[ob] = code_r[e];
+            out_coords[2 * ob] = (I)(s * br);
+            out_coords[2 * ob + 1] = (I)(bcol_r[e] * bc);
+            out_offsets[ob] = (I)(packed_base + doff);
+        }
+        tau[e] = slot;
+        g[e] = doff;
+    }
+    Team<TEAM>::sync();
 }
 
 template <typename I, typename S>
@@ -283,111 +421,62 @@ build_fill_kernel(const I* indptr, const I* indices, const S* values, int64_t ro
         const int64_t rbase = w.stripe_m[s];
         const int m = (int)(w.stripe_m[s + 1] - rbase);
         const int64_t kept_base = w.stripe_kept[s];
-        const int64_t packed_base = w.stripe_packed[s];
         if (lane == 0 && out_stripe_ptr) out_stripe_ptr[s] = (int32_t)kept_base;
-        if (m == 0) continue;
+        if (m == 0 || m > kSmallStripeBlocks) continue;   // big stripes: build_fill_big_kernel
+        record_blocks<I>(indptr, indices, s, rows, cols, nnz, br, bc, w.rec_code + rbase, w.rec_bcol + rbase,
+                         w.rec_ins + rbase);
+        __syncwarp();
+        order_stripe<32, I>(s, m, br, bc, min_nnz, ncb, key32, nchain, w.chain, w.stripe_prefmax[s], kept_base,
+                            w.stripe_packed[s], w.rec_code + rbase, w.rec_bcol + rbase, w.rec_ins + rbase,
+                            w.rec_tau + rbase, w.rec_bkt + rbase, w.rec_g + rbase, w.rec_pos + rbase,
+                            w.rec_pops + rbase, out_codes, out_coords, out_offsets);
+        move_values<I, S>(indptr, indices, values, s, rows, cols, nnz, br, bc, w.rec_tau + rbase, w.rec_g + rbase,
+                          w.stripe_packed[s], w.row_rem, out_data, out_rem_col, out_rem_val);
+    }
+}
 
-        uint64_t* code_r = w.rec_code + rbase;
-        int64_t* bcol_r = w.rec_bcol + rbase;
-        int32_t* ins_r = w.rec_ins + rbase;
-        int32_t* tau_r = w.rec_tau + rbase;
-        uint32_t* bkt_r = w.rec_bkt + rbase;
-        int32_t* g_r = w.rec_g + rbase;
-        int32_t* pos_r = w.rec_pos + rbase;
-
-        // 1. record the distinct blocks in block-column order
-        {
-            StripeMerge<I> mg;
-            mg.init(indptr, indices, s, rows, nnz, br, bc, false);
-            int64_t bcol, first, my_first;
-            uint64_t code;
-            int my_count;
-            int j = 0;
-            while (mg.step(cols, bcol, code, first, my_count, my_first)) {
-                if (lane == 0) {
-                    code_r[j] = code;
-                    bcol_r[j] = bcol;
-                    ins_r[j] = (int32_t)(first - (int64_t)indptr[s * br]);
-                }
-                ++j;
+template <typename I, typename S>
+__global__ void __launch_bounds__(kBigThreads)
+build_fill_big_kernel(const I* indptr, const I* indices, const S* values, int64_t rows, int64_t cols, int64_t nnz,
+                      int br, int bc, int min_nnz, int64_t nstripes, int64_t ncb, bool key32, int nchain,
+                      BuildWs w, uint64_t* out_codes, I* out_coords, I* out_offsets, S* out_data,
+                      I* out_rem_col, S* out_rem_val) {
+    __shared__ int32_t sh_ins[kBigStage], sh_tau[kBigStage], sh_g[kBigStage], sh_pos[kBigStage];
+    __shared__ int32_t sh_pops[kBigStage];
+    __shared__ uint32_t sh_bkt[kBigStage];
+    for (int64_t s = blockIdx.x; s < nstripes; s += gridDim.x) {
+        const int64_t rbase = w.stripe_m[s];
+        const int m = (int)(w.stripe_m[s + 1] - rbase);
+        if (m <= kSmallStripeBlocks) continue;
+        if (threadIdx.x < 32)
+            record_blocks<I>(indptr, indices, s, rows, cols, nnz, br, bc, w.rec_code + rbase, w.rec_bcol + rbase,
+                             w.rec_ins + rbase);
+        __syncthreads();
+        const bool staged = m <= kBigStage;
+        int32_t* ins = staged ? sh_ins : w.rec_ins + rbase;
+        int32_t* tau = staged ? sh_tau : w.rec_tau + rbase;
+        int32_t* g = staged ? sh_g : w.rec_g + rbase;
+        int32_t* pos = staged ? sh_pos : w.rec_pos + rbase;
+        int32_t* pops = staged ? sh_pops : w.rec_pops + rbase;
+        uint32_t* bkt = staged ? sh_bkt : w.rec_bkt + rbase;
+        if (staged)
+            for (int e = threadIdx.x; e < m; e += kBigThreads) ins[e] = w.rec_ins[rbase + e];
+        __syncthreads();
+        order_stripe<kBigThreads, I>(s, m, br, bc, min_nnz, ncb, key32, nchain, w.chain, w.stripe_prefmax[s],
+                                     w.stripe_kept[s], w.stripe_packed[s], w.rec_code + rbase, w.rec_bcol + rbase,
+                                     ins, tau, bkt, g, pos, pops, out_codes, out_coords, out_offsets);
+        // slot -> tau, value offset -> g; move_values reads them from global
+        if (staged) {
+            for (int e = threadIdx.x; e < m; e += kBigThreads) {
+                w.rec_tau[rbase + e] = tau[e];
+                w.rec_g[rbase + e] = g[e];
             }
         }
-        __syncwarp();
-        // 2. insertion rank = rank of the first-nonzero position
-        for (int e = lane; e < m; e += 32) {
-            const int32_t fe = ins_r[e];
-            int r = 0;
-            for (int f = 0; f < m; ++f) r += ins_r[f] < fe;
-            tau_r[e] = r;
-        }
-        __syncwarp();
-        for (int e = lane; e < m; e += 32) ins_r[e] = tau_r[e];
-        __syncwarp();
-        // 3. bucket count at stripe start, rehashes inside the stripe
-        const int64_t M = w.stripe_prefmax[s];
-        int J = 0;
-        while (J + 1 < nchain && w.chain[2 * (J + 1)] <= M) ++J;
-        while (J + 1 < nchain && w.chain[2 * (J + 1)] <= m) {
-            const int present = (int)(w.chain[2 * (J + 1)] - 1);
-            list_order(s, ncb, key32, (uint64_t)w.chain[2 * J + 1], m, present, bcol_r, ins_r, tau_r,
-                       bkt_r, g_r, pos_r);
-            for (int e = lane; e < m; e += 32)
-                if (ins_r[e] < present) tau_r[e] = pos_r[e];
-            __syncwarp();
-            ++J;
-        }
-        list_order(s, ncb, key32, (uint64_t)w.chain[2 * J + 1], m, m, bcol_r, ins_r, tau_r, bkt_r, g_r,
-                   pos_r);
-        // 4. output slot and data offset of each kept block, in list order
-        for (int e = lane; e < m; e += 32) {
-            const bool kept_e = __popcll(code_r[e]) >= min_nnz;
-            int slot = -1, doff = 0;
-            if (kept_e) {
-                slot = 0;
-                const int32_t pe = pos_r[e];
-                for (int f = 0; f < m; ++f) {
-                    const int pf = __popcll(code_r[f]);
-                    if (pf >= min_nnz && pos_r[f] < pe) {
-                        ++slot;
-                        doff += pf;
-                    }
-                }
-                const int64_t ob = kept_base + slot;
-                out_codes[ob] = code_r[e];
-                out_coords[2 * ob] = (I)(s * br);
-                out_coords[2 * ob + 1] = (I)(bcol_r[e] * bc);
-                out_offsets[ob] = (I)(packed_base + doff);
-            }
-            tau_r[e] = slot;
-            g_r[e] = doff;
-        }
-        __syncwarp();
-        // 5. merge again and move the values
-        {
-            StripeMerge<I> mg;
-            mg.init(indptr, indices, s, rows, nnz, br, bc, false);
-            const int64_t row = s * br + lane;
-            int64_t rem_cursor = (lane < br && row < rows) ? w.row_rem[row] : 0;
-            int64_t bcol, first, my_first;
-            uint64_t code;
-            int my_count;
-            int j = 0;
-            while (mg.step(cols, bcol, code, first, my_count, my_first)) {
-                const int slot = tau_r[j];
-                if (slot >= 0) {
-                    const int before = (int)warp_incl_scan_i64(my_count) - my_count;
-                    const int64_t dst = packed_base + g_r[j] + before;
-                    for (int i = 0; i < my_count; ++i) out_data[dst + i] = values[my_first + i];
-                } else {
-                    for (int i = 0; i < my_count; ++i) {
-                        out_rem_col[rem_cursor + i] = indices[my_first + i];
-                        out_rem_val[rem_cursor + i] = values[my_first + i];
-                    }
-                    rem_cursor += my_count;
-                }
-                ++j;
-            }
-        }
+        __syncthreads();
+        if (threadIdx.x < 32)
+            move_values<I, S>(indptr, indices, values, s, rows, cols, nnz, br, bc, w.rec_tau + rbase,
+                              w.rec_g + rbase, w.stripe_packed[s], w.row_rem, out_data, out_rem_col, out_rem_val);
+        __syncthreads();
     }
 }
 
@@ -520,6 +609,13 @@ int fill_impl(const I* indptr, const I* indices, const S* values, int64_t rows, 
             indptr, indices, values, rows, cols, nnz, br, bc, min_nnz, ns, (int64_t)ncb, sizeof(I) == 4, nchain, w, codes,
             coords, offsets, data, rem_col, rem_val, stripe_ptr);
         GL_LAUNCH_CHECK("build_fill_kernel");
+        if (counts->max_stripe_blocks > kSmallStripeBlocks) {
+            const int64_t big_blocks = (int64_t)num_sms() * 2;
+            build_fill_big_kernel<I, S><<<(unsigned)big_blocks, kBigThreads, 0, stream>>>(
+                indptr, indices, values, rows, cols, nnz, br, bc, min_nnz, ns, (int64_t)ncb, sizeof(I) == 4, nchain,
+                w, codes, coords, offsets, data, rem_col, rem_val);
+            GL_LAUNCH_CHECK("build_fill_big_kernel");
+        }
     }
     finish_kernel<I><<<(unsigned)ceil_div(rows + 1, 256), 256, 0, stream>>>(w, rows, ns, offsets, rem_indptr,
                                                                             stripe_ptr);

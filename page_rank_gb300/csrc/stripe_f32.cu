@@ -5,35 +5,37 @@ namespace gl {
 
 namespace {
 template <bool PPR, int BR>
-int dispatch_f32(const StripeArgs<float>& a, cudaStream_t st) {
-    const int K = a.K;
-    if (K >= 128 && pick_vec(a, 4) == 4) return launch_stripe_shape<float, BR, 4, 32, PPR>(a, st);
-    if (K >= 64 && pick_vec(a, 2) >= 2) return launch_stripe_shape<float, BR, 2, 32, PPR>(a, st);
-    if (K >= 17) return launch_stripe_shape<float, BR, 1, 32, PPR>(a, st);
-    if (K >= 9) return launch_stripe_shape<float, BR, 1, 16, PPR>(a, st);
-    if (K >= 5) return launch_stripe_shape<float, BR, 1, 8, PPR>(a, st);
-    if (K >= 3) return launch_stripe_shape<float, BR, 1, 4, PPR>(a, st);
-    if (K == 2) return launch_stripe_shape<float, BR, 1, 2, PPR>(a, st);
-    return launch_stripe_shape<float, BR, 1, 1, PPR>(a, st);
+int dispatch_f32(const StripeArgs<float>& a, int tile_hint, cudaStream_t st) {
+    const Shape sh = pick_shape<float>(a.K, tile_hint, a.X, a.Y);
+    switch (sh.V * 100 + sh.C) {
+        case 432: return launch_stripe_shape<float, BR, 4, 32, PPR>(a, st);
+        case 232: return launch_stripe_shape<float, BR, 2, 32, PPR>(a, st);
+        case 132: return launch_stripe_shape<float, BR, 1, 32, PPR>(a, st);
+        case 116: return launch_stripe_shape<float, BR, 1, 16, PPR>(a, st);
+        case 108: return launch_stripe_shape<float, BR, 1, 8, PPR>(a, st);
+        case 104: return launch_stripe_shape<float, BR, 1, 4, PPR>(a, st);
+        case 102: return launch_stripe_shape<float, BR, 1, 2, PPR>(a, st);
+        default: return launch_stripe_shape<float, BR, 1, 1, PPR>(a, st);
+    }
 }
 }  // namespace
 
 template <bool PPR>
-static int launch_f32(const StripeArgs<float>& a, int br, int bc, cudaStream_t st) {
-    if (br == 2 && bc == 2) return dispatch_f32<PPR, 2>(a, st);
-    if (br == 4 && bc == 4) return dispatch_f32<PPR, 4>(a, st);
-    if (br == 8 && bc == 8) return dispatch_f32<PPR, 8>(a, st);
+static int launch_f32(const StripeArgs<float>& a, int br, int bc, int tile_hint, cudaStream_t st) {
+    if (br == 2 && bc == 2) return dispatch_f32<PPR, 2>(a, tile_hint, st);
+    if (br == 4 && bc == 4) return dispatch_f32<PPR, 4>(a, tile_hint, st);
+    if (br == 8 && bc == 8) return dispatch_f32<PPR, 8>(a, tile_hint, st);
     set_error("Unsupported block size for PBR SpMM. Only 2x2, 4x4, and 8x8 are supported.");
     return GL_ERR_UNSUPPORTED_BLOCK;
 }
 
 template <>
-int launch_stripe<float, false>(const StripeArgs<float>& a, int br, int bc, cudaStream_t st) {
-    return launch_f32<false>(a, br, bc, st);
+int launch_stripe<float, false>(const StripeArgs<float>& a, int br, int bc, int tile_hint, cudaStream_t st) {
+    return launch_f32<false>(a, br, bc, tile_hint, st);
 }
 template <>
-int launch_stripe<float, true>(const StripeArgs<float>& a, int br, int bc, cudaStream_t st) {
-    return launch_f32<true>(a, br, bc, st);
+int launch_stripe<float, true>(const StripeArgs<float>& a, int br, int bc, int tile_hint, cudaStream_t st) {
+    return launch_f32<true>(a, br, bc, tile_hint, st);
 }
 
 }  // namespace gl

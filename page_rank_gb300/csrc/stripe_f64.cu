@@ -6,30 +6,30 @@ namespace gl {
 
 namespace {
 template <bool PPR, int BR>
-int dispatch_f64(const StripeArgs<double>& a, cudaStream_t st) {
-    const int K = a.K;
-    if (K >= 64 && pick_vec(a, 2) == 2) return launch_stripe_shape<double, BR, 2, 32, PPR>(a, st);
-    if (K >= 17) return launch_stripe_shape<double, BR, 1, 32, PPR>(a, st);
+int dispatch_f64(const StripeArgs<double>& a, int tile_hint, cudaStream_t st) {
+    const Shape sh = pick_shape<double>(a.K, tile_hint, a.X, a.Y);
+    if (sh.C == 32 && sh.V == 2) return launch_stripe_shape<double, BR, 2, 32, PPR>(a, st);
+    if (sh.C == 32) return launch_stripe_shape<double, BR, 1, 32, PPR>(a, st);
     return launch_stripe_shape<double, BR, 1, 1, PPR>(a, st);
 }
 }  // namespace
 
 template <bool PPR>
-static int launch_f64(const StripeArgs<double>& a, int br, int bc, cudaStream_t st) {
-    if (br == 2 && bc == 2) return dispatch_f64<PPR, 2>(a, st);
-    if (br == 4 && bc == 4) return dispatch_f64<PPR, 4>(a, st);
-    if (br == 8 && bc == 8) return dispatch_f64<PPR, 8>(a, st);
+static int launch_f64(const StripeArgs<double>& a, int br, int bc, int tile_hint, cudaStream_t st) {
+    if (br == 2 && bc == 2) return dispatch_f64<PPR, 2>(a, tile_hint, st);
+    if (br == 4 && bc == 4) return dispatch_f64<PPR, 4>(a, tile_hint, st);
+    if (br == 8 && bc == 8) return dispatch_f64<PPR, 8>(a, tile_hint, st);
     set_error("Unsupported block size for PBR SpMM. Only 2x2, 4x4, and 8x8 are supported.");
     return GL_ERR_UNSUPPORTED_BLOCK;
 }
 
 template <>
-int launch_stripe<double, false>(const StripeArgs<double>& a, int br, int bc, cudaStream_t st) {
-    return launch_f64<false>(a, br, bc, st);
+int launch_stripe<double, false>(const StripeArgs<double>& a, int br, int bc, int tile_hint, cudaStream_t st) {
+    return launch_f64<false>(a, br, bc, tile_hint, st);
 }
 template <>
-int launch_stripe<double, true>(const StripeArgs<double>& a, int br, int bc, cudaStream_t st) {
-    return launch_f64<true>(a, br, bc, st);
+int launch_stripe<double, true>(const StripeArgs<double>& a, int br, int bc, int tile_hint, cudaStream_t st) {
+    return launch_f64<true>(a, br, bc, tile_hint, st);
 }
 
 }  // namespace gl

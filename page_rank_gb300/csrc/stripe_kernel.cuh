@@ -1,18 +1,34 @@
 // Stripe-owning fused PBR-block + CSR-remainder kernel (sm_103a).
 //
-// One "group" of G lanes owns one output stripe (block_rows consecutive rows)
-// for one column tile of T = G * V columns; each lane owns V consecutive
-// columns and keeps block_rows x V accumulators in registers.  For every
-// block of the stripe the lane stages the X rows of the block's active
-// columns (one vector load per column) in its own shared-memory slots, then
-// walks the set bits of the 64-bit code row by row; the packed values are in
-// row-major bit order, so the value index is a running counter.  The CSR
-// remainder rows of the stripe are then added by the same lane, and the tile
-// is written once: no atomics, no pre-zeroed output, no second stream.
+// Work unit: one warp owns one output stripe (block_rows consecutive rows)
+// for one column tile.  The warp's 32 lanes form C column lanes x P nonzero
+// lanes (C * P = 32): column lane c owns V consecutive columns of the tile
+// (T = C * V columns per tile), and the P nonzero lanes split the stripe's
+// blocks and remainder entries between them.  Each lane keeps
+// block_rows x V accumulators in registers; at the end the P partial sums
+// are folded with warp shuffles and the tile is written once — no atomics on
+// the output, no pre-zeroed output, no second stream.
 //
-// With PPR = true the epilogue is one power-iteration step instead of a plain
-// store: X_out = alpha * (A X_in) + scale_k * teleport, the L1 change per
-// column and the dangling mass of X_out are accumulated in the same pass.
+//   * PBR blocks: the lane stages the X rows of the block's active columns
+//     (one vector load each, all issued before use) in its own shared-memory
+//     slots, then walks the set bits of the 64-bit code row by row; values
+//     are packed in row-major bit order, so the value index is a counter.
+//     With P == 1 the warp loads the metadata of 32 blocks at once and
+//     broadcasts it with shuffles.
+//   * CSR remainder: row by row; with P == 1 the warp loads 32 (column,
+//     value) pairs at once and issues the X-row gathers eight at a time.
+//
+// Load balance: stripes whose stored entries exceed 2 x piece_work (R-MAT
+// hub rows reach tens of thousands) are cut into pieces of piece_work
+// entries (packed values first, then remainder entries).  A piece is an
+// independent work unit; each piece writes its partial tile to the caller's
+// workspace, and the warp that finishes a stripe's last piece (detected with
+// a per-stripe counter after a memory fence; nobody waits) adds the partials
+// in piece order — so results are deterministic — and runs the epilogue.
+//
+// With PPR = true the epilogue is one power-iteration step instead of a
+// plain store: X_out = alpha * (A X_in) + teleport terms, with the L1 change
+// per column and the dangling mass of X_out accumulated in the same pass.
 //
 // The reference splits this work over two kernels on two streams with global
 // atomics (kernels/pbr_kernel.cu:12-333 block kernels, :421-458 CSR kernel,
@@ -25,6 +41,7 @@
 namespace gl {
 
 constexpr int kStripeThreads = 256;
+constexpr int kStripeWarps = kStripeThreads / 32;
 
 template <typename S, int V>
 struct alignas(sizeof(S) * V) Pack {
@@ -45,6 +62,14 @@ struct StripeArgs {
     int32_t K, ntiles;
     const S* X;
     S* Y;
+    // heavy-stripe schedule (num_pieces == 0: every stripe is one unit)
+    int32_t num_pieces, piece_work;
+    const int32_t* heavy_of;       // [nstripes] heavy index or -1
+    const int32_t* heavy_stripe;   // [num_heavy]
+    const int32_t* heavy_first;    // [num_heavy + 1]
+    const int32_t* piece_heavy;    // [num_pieces]
+    S* partial;                    // [num_pieces][batch * ntiles][BR][T]
+    int32_t* counters;             // [num_heavy][batch * ntiles], zero between calls
     // power-iteration epilogue
     const int32_t* tp_ptr;
     const int32_t* tp_row;
@@ -56,6 +81,7 @@ struct StripeArgs {
     double* res_hist;
     double* dang_hist;
     const uint32_t* dbitmap;
+    int32_t dang_uniform;
 };
 
 template <typename S, int V>
@@ -63,26 +89,197 @@ __device__ __forceinline__ Pack<S, V> load_pack(const S* p) {
     return *reinterpret_cast<const Pack<S, V>*>(p);
 }
 template <typename S, int V>
+__device__ __forceinline__ Pack<S, V> load_pack_cg(const S* p) {
+    Pack<S, V> r;
+#pragma unroll
+    for (int j = 0; j < V; ++j) r.v[j] = __ldcg(p + j);
+    return r;
+}
+template <typename S, int V>
 __device__ __forceinline__ void store_pack(S* p, const Pack<S, V>& v) {
     *reinterpret_cast<Pack<S, V>*>(p) = v;
 }
 
-template <typename S, int BR, int BC, int V, int G, bool PPR>
+// First index in [lo, hi) with offsets[idx] >= key (hi if none).
+__device__ __forceinline__ int32_t lower_bound_i32(const int32_t* offsets, int32_t lo, int32_t hi, int64_t key) {
+    while (lo < hi) {
+        const int32_t mid = lo + ((hi - lo) >> 1);
+        if ((int64_t)offsets[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------------------------
+// Asynchronous gather pipeline for P == 1 (one warp = one stripe, every lane
+// owns V columns).  The stripe's work is a sequence of "groups": one group per
+// PBR block (the X rows of its active columns) followed by groups of
+// kRemGroup remainder entries.  Each group's X-row pieces are copied global
+// -> shared with cp.async (LDGSTS, one 4/8/16-byte copy per lane per row)
+// into the lane's own slots of pipeline stage g % stages; kStages groups are
+// in flight while the oldest is consumed.  cp.async.wait_group is a hardware
+// wait (no software spin).  Each lane reads back only its own slots, so no
+// barrier is needed between lanes.
+// ---------------------------------------------------------------------------
+constexpr int kRemGroup = 8;
+template <int V>
+struct PipeCfg {
+    static constexpr int kStages = V >= 4 ? 2 : 3;
+    static constexpr int kSlots = 8;   // max(block columns, kRemGroup)
+};
+
+template <int BYTES>
+__device__ __forceinline__ void cp_async_lane(void* smem, const void* gmem) {
+    const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(dst), "l"(gmem), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <typename S, int BR, int BC, int V>
+__device__ __forceinline__ void accumulate_pipelined(const StripeArgs<S>& a, S (&acc)[BR][V], unsigned char* xs_raw,
+                                                     int64_t s, int32_t b0, int32_t b1, int32_t j0, int32_t j1,
+                                                     const S* __restrict__ Xb, bool lane_ok, int lane) {
+    constexpr int ST = PipeCfg<V>::kStages;
+    constexpr int SL = PipeCfg<V>::kSlots;
+    constexpr int BYTES = V * (int)sizeof(S);
+    constexpr uint32_t ROWMASK = (BC >= 32) ? 0xffffffffu : ((1u << BC) - 1u);
+    Pack<S, V>* xs = reinterpret_cast<Pack<S, V>*>(xs_raw);
+    auto slot = [&](int stage, int k) -> Pack<S, V>* {
+        return xs + ((size_t)(stage * SL + k) * kStripeThreads + threadIdx.x);
+    };
+    // end of each stripe row inside the remainder range, for entry -> row
+    int32_t row_end[BR];
+#pragma unroll
+    for (int r = 0; r < BR; ++r) {
+        const int64_t row = s * BR + r;
+        row_end[r] = (row < a.rows) ? a.rem_ptr[row + 1] : j1;
+    }
+    const int32_t n_rem_groups = (j1 - j0 + kRemGroup - 1) / kRemGroup;
+
+    for (int32_t kc = b0; kc < b1 || kc == b0; kc += 32) {
+        // blocks of this 32-chunk (metadata in lane registers), plus the
+        // remainder groups when this is the last chunk
+        const int32_t nb = (b1 - kc) < 32 ? (b1 - kc > 0 ? b1 - kc : 0) : 32;
+        const bool last_chunk = kc + 32 >= b1;
+        uint64_t m_code = 0;
+        int32_t m_col = 0, m_off = 0;
+        if (lane < nb) {
+            m_code = static_cast<uint64_t>(a.codes[kc + lane]);
+            m_col = a.coords[2 * (int64_t)(kc + lane) + 1];
+            m_off = a.offsets[kc + lane];
+        }
+        const int32_t ng = nb + (last_chunk ? n_rem_groups : 0);
+
+        auto issue = [&](int32_t g) {
+            if (g < ng) {                       // warp-uniform
+                const int stage = g % ST;
+                if (g < nb) {
+                    const uint64_t code = __shfl_sync(0xffffffffu, m_code, g);
+                    const int64_t col0 = __shfl_sync(0xffffffffu, m_col, g);
+                    if (lane_ok) {
+                        uint32_t colmask = 0;
+#pragma unroll
+                        for (int r = 0; r < BR; ++r) colmask |= (uint32_t)(code >> (r * BC)) & ROWMASK;
+#pragma unroll
+                        for (int c = 0; c < BC; ++c)
+                            if ((colmask >> c) & 1u) cp_async_lane<BYTES>(slot(stage, c), Xb + (col0 + c) * a.K);
+                    }
+                } else if (lane_ok) {
+                    const int32_t jg = j0 + (g - nb) * kRemGroup;
+                    const int32_t cnt = (j1 - jg) < kRemGroup ? (j1 - jg) : kRemGroup;
+#pragma unroll
+                    for (int q = 0; q < kRemGroup; ++q)
+                        if (q < cnt) cp_async_lane<BYTES>(slot(stage, q), Xb + (int64_t)a.rem_col[jg + q] * a.K);
+                }
+            }
+            cp_async_commit();
+        };
+
+#pragma unroll
+        for (int g = 0; g < ST - 1; ++g) issue(g);
+        for (int32_t g = 0; g < ng; ++g) {
+            issue(g + ST - 1);
+            cp_async_wait<ST - 1>();
+            const int stage = g % ST;
+            if (g < nb) {
+                const uint64_t code = __shfl_sync(0xffffffffu, m_code, g);
+                int32_t k = __shfl_sync(0xffffffffu, m_off, g);
+#pragma unroll
+                for (int r = 0; r < BR; ++r) {
+                    uint32_t bits = (uint32_t)(code >> (r * BC)) & ROWMASK;
+                    while (bits) {
+                        const int c = __ffs(bits) - 1;
+                        bits &= bits - 1u;
+                        const S v = a.bdata[k++];
+                        if (lane_ok) {
+                            const Pack<S, V> x = *slot(stage, c);
+#pragma unroll
+                            for (int j = 0; j < V; ++j) acc[r][j] = fma(v, x.v[j], acc[r][j]);
+                        }
+                    }
+                }
+            } else {
+                const int32_t jg = j0 + (g - nb) * kRemGroup;
+                const int32_t cnt = (j1 - jg) < kRemGroup ? (j1 - jg) : kRemGroup;
+                // lane q < cnt fetches value and row of entry jg + q
+                S my_v = S(0);
+                int my_r = 0;
+                if (lane < cnt) {
+                    const int32_t j = jg + lane;
+                    my_v = a.rem_val[j];
+#pragma unroll
+                    for (int r = 0; r < BR - 1; ++r) my_r += (j >= row_end[r]) ? 1 : 0;
+                }
+#pragma unroll
+                for (int q = 0; q < kRemGroup; ++q) {
+                    if (q < cnt) {
+                        const S v = __shfl_sync(0xffffffffu, my_v, q);
+                        const int rq = __shfl_sync(0xffffffffu, my_r, q);
+                        if (lane_ok) {
+                            const Pack<S, V> x = *slot(stage, q);
+#pragma unroll
+                            for (int r = 0; r < BR; ++r)
+                                if (r == rq) {
+#pragma unroll
+                                    for (int j = 0; j < V; ++j) acc[r][j] = fma(v, x.v[j], acc[r][j]);
+                                }
+                        }
+                    }
+                }
+            }
+        }
+        cp_async_wait<0>();
+        if (kc >= b1) break;   // empty block range: one pass for the remainder
+    }
+}
+
+// Dynamic shared memory of one CTA of stripe_kernel.
+template <typename S, int BC, int V, int C>
+constexpr size_t stripe_smem_bytes() {
+    return (32 / C == 1) ? (size_t)PipeCfg<V>::kStages * PipeCfg<V>::kSlots * kStripeThreads * V * sizeof(S)
+                         : (size_t)BC * kStripeThreads * V * sizeof(S);
+}
+
+template <typename S, int BR, int BC, int V, int C, bool PPR>
 __global__ void __launch_bounds__(kStripeThreads)
 stripe_kernel(const StripeArgs<S> a) {
-    constexpr int T = G * V;            // columns per group
-    constexpr int GPW = 32 / G;         // groups per warp
+    constexpr int P = 32 / C;            // nonzero lanes per warp
+    constexpr int T = C * V;             // columns per tile
     constexpr uint32_t ROWMASK = (BC >= 32) ? 0xffffffffu : ((1u << BC) - 1u);
 
-    __shared__ Pack<S, V> xs[BC][kStripeThreads];
+    extern __shared__ __align__(16) unsigned char xs_dyn[];
     __shared__ int s_skip;
 
     const int lane = threadIdx.x & 31;
-    const int gl_lane = lane % G;
-    const int64_t gid = ((int64_t)blockIdx.x * (kStripeThreads / 32) + (threadIdx.x >> 5)) * GPW + lane / G;
-    const int64_t ngroups = (int64_t)gridDim.x * (kStripeThreads / 32) * GPW;
+    const int c_lane = lane % C;
+    const int p_lane = lane / C;
+    const int64_t warp_id = (int64_t)blockIdx.x * kStripeWarps + (threadIdx.x >> 5);
+    const int64_t nwarps = (int64_t)gridDim.x * kStripeWarps;
     const int64_t BT = a.batch * a.ntiles;
-    const int64_t items = a.nstripes * BT;
+    const int64_t units = (int64_t)a.num_pieces + a.nstripes;
+    const int64_t items = units * BT;
 
     int t = 0;
     if constexpr (PPR) {
@@ -107,11 +304,18 @@ stripe_kernel(const StripeArgs<S> a) {
     int cur_col = 0;
     bool cur_ok = false;
     S scale[V];
+    S unif[V];
     bool frozen[V];
     float res_acc[V];
     float dang_acc[V];
 #pragma unroll
-    for (int j = 0; j < V; ++j) { scale[j] = S(0); frozen[j] = false; res_acc[j] = 0.f; dang_acc[j] = 0.f; }
+    for (int j = 0; j < V; ++j) {
+        scale[j] = S(0);
+        unif[j] = S(0);
+        frozen[j] = false;
+        res_acc[j] = 0.f;
+        dang_acc[j] = 0.f;
+    }
 
     auto flush = [&]() {
         if constexpr (PPR) {
@@ -129,27 +333,67 @@ stripe_kernel(const StripeArgs<S> a) {
         }
     };
 
-    for (int64_t item = gid; item < items; item += ngroups) {
-        const int64_t s = item / BT;
-        const int64_t bt = item - s * BT;
+    for (int64_t item = warp_id; item < items; item += nwarps) {
+        const int64_t u = item / BT;
+        const int64_t bt = item - u * BT;
         const int64_t b = bt / a.ntiles;
         const int tile = (int)(bt - b * a.ntiles);
-        const int col_base = tile * T + gl_lane * V;
+        const int col_base = tile * T + c_lane * V;
         const bool lane_ok = col_base < a.K;
+
+        // ---- the unit: a light stripe or one piece of a heavy stripe -------
+        int64_t s;
+        int32_t b0, b1, j0, j1;
+        int32_t h = -1, pidx = 0, npieces = 1;
+        if (u < a.num_pieces) {
+            h = a.piece_heavy[u];
+            s = a.heavy_stripe[h];
+            const int32_t f0 = a.heavy_first[h];
+            pidx = (int32_t)(u - f0);
+            npieces = a.heavy_first[h + 1] - f0;
+            const int32_t sb0 = a.stripe_ptr[s], sb1 = a.stripe_ptr[s + 1];
+            const int64_t pk0 = a.offsets[sb0];
+            const int64_t pw = (int64_t)a.offsets[sb1] - pk0;
+            const int64_t last_row = (s * BR + BR < a.rows) ? s * BR + BR : a.rows;
+            const int32_t rj0 = a.rem_ptr[s * BR], rj1 = a.rem_ptr[last_row];
+            const int64_t total = pw + (rj1 - rj0);
+            const int64_t u0 = (int64_t)pidx * a.piece_work;
+            const int64_t u1 = (u0 + a.piece_work < total) ? u0 + a.piece_work : total;
+            b0 = lower_bound_i32(a.offsets, sb0, sb1, pk0 + u0);
+            b1 = (u1 >= pw) ? sb1 : lower_bound_i32(a.offsets, sb0, sb1, pk0 + u1);
+            const int64_t r0 = u0 > pw ? u0 - pw : 0;
+            const int64_t r1 = u1 > pw ? u1 - pw : 0;
+            j0 = rj0 + (int32_t)r0;
+            j1 = rj0 + (int32_t)r1;
+        } else {
+            s = u - a.num_pieces;
+            if (a.heavy_of != nullptr && a.heavy_of[s] >= 0) continue;
+            b0 = a.stripe_ptr[s];
+            b1 = a.stripe_ptr[s + 1];
+            const int64_t last_row = (s * BR + BR < a.rows) ? s * BR + BR : a.rows;
+            j0 = a.rem_ptr[s * BR];
+            j1 = a.rem_ptr[last_row];
+        }
 
         if constexpr (PPR) {
             if (bt != cur_bt) {
                 flush();
                 cur_bt = bt;
                 cur_col = col_base;
-                cur_ok = lane_ok;
+                cur_ok = lane_ok && p_lane == 0;
                 if (lane_ok) {
 #pragma unroll
                     for (int j = 0; j < V; ++j) {
                         const int col = col_base + j;
                         double sc = 1.0 - a.alpha;
-                        if (a.dbitmap != nullptr) sc += a.alpha * a.dang_hist[(int64_t)t * a.K + col];
+                        double un = 0.0;
+                        if (a.dbitmap != nullptr) {
+                            const double d = a.alpha * a.dang_hist[(int64_t)t * a.K + col];
+                            if (a.dang_uniform) un = d / (double)a.rows;
+                            else sc += d;
+                        }
                         scale[j] = static_cast<S>(sc);
+                        unif[j] = static_cast<S>(un);
                         frozen[j] = (a.stop_mode == GL_PPR_STOP_PER_COLUMN && t > 0 &&
                                      a.res_hist[(int64_t)(t - 1) * a.K + col] < a.tol);
                     }
@@ -165,78 +409,133 @@ stripe_kernel(const StripeArgs<S> a) {
 
         const S* __restrict__ Xb = a.X + b * a.cols * (int64_t)a.K + col_base;
 
-        // ---- PBR blocks of this stripe ------------------------------------
-        const int32_t kb0 = a.stripe_ptr[s];
-        const int32_t kb1 = a.stripe_ptr[s + 1];
-        for (int32_t kb = kb0; kb < kb1; ++kb) {
-            const uint64_t code = static_cast<uint64_t>(a.codes[kb]);
-            const int64_t col0 = a.coords[2 * (int64_t)kb + 1];
-            int32_t k = a.offsets[kb];
-            uint32_t colmask = 0;
+        if constexpr (P == 1) {
+            accumulate_pipelined<S, BR, BC, V>(a, acc, xs_dyn, s, b0, b1, j0, j1, Xb, lane_ok, lane);
+        } else {
+            // ---- PBR blocks: lanes stride the blocks ------------------------
+            for (int32_t kb = b0 + p_lane; kb < b1; kb += P) {
+                const uint64_t code = static_cast<uint64_t>(a.codes[kb]);
+                const int64_t col0 = a.coords[2 * (int64_t)kb + 1];
+                int32_t k = a.offsets[kb];
+                uint32_t colmask = 0;
 #pragma unroll
-            for (int r = 0; r < BR; ++r) colmask |= (uint32_t)(code >> (r * BC)) & ROWMASK;
-            if (lane_ok) {
+                for (int r = 0; r < BR; ++r) colmask |= (uint32_t)(code >> (r * BC)) & ROWMASK;
+                Pack<S, V>* xs = reinterpret_cast<Pack<S, V>*>(xs_dyn);
+                if (lane_ok) {
 #pragma unroll
-                for (int c = 0; c < BC; ++c)
-                    if ((colmask >> c) & 1u)
-                        xs[c][threadIdx.x] = load_pack<S, V>(Xb + (col0 + c) * a.K);
-            }
+                    for (int c = 0; c < BC; ++c)
+                        if ((colmask >> c) & 1u)
+                            xs[c * kStripeThreads + threadIdx.x] = load_pack<S, V>(Xb + (col0 + c) * a.K);
+                }
 #pragma unroll
-            for (int r = 0; r < BR; ++r) {
-                uint32_t bits = (uint32_t)(code >> (r * BC)) & ROWMASK;
-                while (bits) {
-                    const int c = __ffs(bits) - 1;
-                    bits &= bits - 1u;
-                    const S v = a.bdata[k++];
-                    if (lane_ok) {
-                        const Pack<S, V> x = xs[c][threadIdx.x];
+                for (int r = 0; r < BR; ++r) {
+                    uint32_t bits = (uint32_t)(code >> (r * BC)) & ROWMASK;
+                    while (bits) {
+                        const int c = __ffs(bits) - 1;
+                        bits &= bits - 1u;
+                        const S v = a.bdata[k++];
+                        if (lane_ok) {
+                            const Pack<S, V> x = xs[c * kStripeThreads + threadIdx.x];
 #pragma unroll
-                        for (int j = 0; j < V; ++j) acc[r][j] = fma(v, x.v[j], acc[r][j]);
+                            for (int j = 0; j < V; ++j) acc[r][j] = fma(v, x.v[j], acc[r][j]);
+                        }
                     }
                 }
             }
-        }
-
-        // ---- CSR remainder rows of this stripe ------------------------------
+            // ---- CSR remainder: lanes stride the entries of each row ---------
 #pragma unroll
-        for (int r = 0; r < BR; ++r) {
-            const int64_t row = s * BR + r;
-            if (row < a.rows) {
-                int32_t j = a.rem_ptr[row];
-                const int32_t je = a.rem_ptr[row + 1];
-                for (; j + 4 <= je; j += 4) {
-                    const int64_t c0 = a.rem_col[j], c1 = a.rem_col[j + 1];
-                    const int64_t c2 = a.rem_col[j + 2], c3 = a.rem_col[j + 3];
-                    const S v0 = a.rem_val[j], v1 = a.rem_val[j + 1];
-                    const S v2 = a.rem_val[j + 2], v3 = a.rem_val[j + 3];
+            for (int r = 0; r < BR; ++r) {
+                const int64_t row = s * BR + r;
+                if (row >= a.rows) continue;
+                int32_t rs = a.rem_ptr[row], re = a.rem_ptr[row + 1];
+                rs = rs > j0 ? rs : j0;
+                re = re < j1 ? re : j1;
+                int32_t jj = rs + p_lane;
+                for (; jj + 3 * P < re; jj += 4 * P) {
+                    const int64_t c0 = a.rem_col[jj], c1 = a.rem_col[jj + P];
+                    const int64_t c2 = a.rem_col[jj + 2 * P], c3 = a.rem_col[jj + 3 * P];
+                    const S v0 = a.rem_val[jj], v1 = a.rem_val[jj + P];
+                    const S v2 = a.rem_val[jj + 2 * P], v3 = a.rem_val[jj + 3 * P];
                     if (lane_ok) {
                         const Pack<S, V> x0 = load_pack<S, V>(Xb + c0 * a.K);
                         const Pack<S, V> x1 = load_pack<S, V>(Xb + c1 * a.K);
                         const Pack<S, V> x2 = load_pack<S, V>(Xb + c2 * a.K);
                         const Pack<S, V> x3 = load_pack<S, V>(Xb + c3 * a.K);
 #pragma unroll
-                        for (int q = 0; q < V; ++q) {
-                            acc[r][q] = fma(v0, x0.v[q], acc[r][q]);
-                            acc[r][q] = fma(v1, x1.v[q], acc[r][q]);
-                            acc[r][q] = fma(v2, x2.v[q], acc[r][q]);
-                            acc[r][q] = fma(v3, x3.v[q], acc[r][q]);
+                        for (int j = 0; j < V; ++j) {
+                            acc[r][j] = fma(v0, x0.v[j], acc[r][j]);
+                            acc[r][j] = fma(v1, x1.v[j], acc[r][j]);
+                            acc[r][j] = fma(v2, x2.v[j], acc[r][j]);
+                            acc[r][j] = fma(v3, x3.v[j], acc[r][j]);
                         }
                     }
                 }
-                for (; j < je; ++j) {
-                    const int64_t c0 = a.rem_col[j];
-                    const S v0 = a.rem_val[j];
+                for (; jj < re; jj += P) {
+                    const int64_t c0 = a.rem_col[jj];
+                    const S v0 = a.rem_val[jj];
                     if (lane_ok) {
                         const Pack<S, V> x0 = load_pack<S, V>(Xb + c0 * a.K);
 #pragma unroll
-                        for (int q = 0; q < V; ++q) acc[r][q] = fma(v0, x0.v[q], acc[r][q]);
+                        for (int j = 0; j < V; ++j) acc[r][j] = fma(v0, x0.v[j], acc[r][j]);
                     }
                 }
             }
         }
 
-        if (!lane_ok) continue;
+        // ---- fold the P nonzero lanes ----------------------------------------
+        if constexpr (P > 1) {
+#pragma unroll
+            for (int off = C; off < 32; off <<= 1)
+#pragma unroll
+                for (int r = 0; r < BR; ++r)
+#pragma unroll
+                    for (int j = 0; j < V; ++j) acc[r][j] += __shfl_xor_sync(0xffffffffu, acc[r][j], off);
+        }
 
+        // ---- heavy stripe: publish the partial; the last piece reduces ------
+        if (h >= 0) {
+            S* part = a.partial + ((int64_t)u * BT + bt) * BR * T + c_lane * V;
+            if (p_lane == 0 && lane_ok) {
+#pragma unroll
+                for (int r = 0; r < BR; ++r) {
+                    Pack<S, V> o;
+#pragma unroll
+                    for (int j = 0; j < V; ++j) o.v[j] = acc[r][j];
+                    store_pack<S, V>(part + r * T, o);
+                }
+            }
+            __threadfence();
+            __syncwarp();
+            int last = 0;
+            if (lane == 0) {
+                const int old = atomicAdd(a.counters + (int64_t)h * BT + bt, 1);
+                last = (old == npieces - 1);
+                if (last) a.counters[(int64_t)h * BT + bt] = 0;   // ready for the next call
+            }
+            last = __shfl_sync(0xffffffffu, last, 0);
+            if (!last) continue;
+            __threadfence();
+            const int64_t first = (int64_t)a.heavy_first[h];
+#pragma unroll
+            for (int r = 0; r < BR; ++r)
+#pragma unroll
+                for (int j = 0; j < V; ++j) acc[r][j] = S(0);
+            if (p_lane == 0 && lane_ok) {
+                for (int32_t q = 0; q < npieces; ++q) {
+                    const S* pp = a.partial + ((first + q) * BT + bt) * BR * T + c_lane * V;
+#pragma unroll
+                    for (int r = 0; r < BR; ++r) {
+                        const Pack<S, V> x = load_pack_cg<S, V>(pp + r * T);
+#pragma unroll
+                        for (int j = 0; j < V; ++j) acc[r][j] += x.v[j];
+                    }
+                }
+            }
+        }
+
+        if (!(lane_ok && p_lane == 0)) continue;
+
+        // ---- epilogue --------------------------------------------------------
         if constexpr (!PPR) {
             S* Yb = a.Y + (b * a.rows) * (int64_t)a.K + col_base;
 #pragma unroll
@@ -253,8 +552,7 @@ stripe_kernel(const StripeArgs<S> a) {
 #pragma unroll
             for (int r = 0; r < BR; ++r)
 #pragma unroll
-                for (int j = 0; j < V; ++j) acc[r][j] *= alpha;
-            // teleport entries of this stripe that fall in this lane's columns
+                for (int j = 0; j < V; ++j) acc[r][j] = fma(alpha, acc[r][j], unif[j]);
             const int32_t e0 = a.tp_ptr[s], e1 = a.tp_ptr[s + 1];
             for (int32_t e = e0; e < e1; ++e) {
                 const int rr = a.tp_row[e] - (int)(s * BR);
@@ -275,8 +573,7 @@ stripe_kernel(const StripeArgs<S> a) {
                 const int64_t row = s * BR + r;
                 if (row < a.rows) {
                     const Pack<S, V> old = load_pack<S, V>(Xin + row * a.K);
-                    const bool dang = a.dbitmap != nullptr &&
-                                      ((a.dbitmap[row >> 5] >> (row & 31)) & 1u);
+                    const bool dang = a.dbitmap != nullptr && ((a.dbitmap[row >> 5] >> (row & 31)) & 1u);
                     Pack<S, V> o;
 #pragma unroll
                     for (int j = 0; j < V; ++j) {
@@ -293,9 +590,13 @@ stripe_kernel(const StripeArgs<S> a) {
     flush();
 }
 
-// Host-side launcher for one (S, PPR) family; picks block shape, vector
-// width and group width.  Returns a GL_* status.
+// Host-side launcher for one (S, PPR) family; picks the block shape, the
+// vector width V and the column-lane count C.  Returns a GL_* status.
 template <typename S, bool PPR>
-int launch_stripe(const StripeArgs<S>& a0, int block_rows, int block_cols, cudaStream_t stream);
+int launch_stripe(const StripeArgs<S>& a0, int block_rows, int block_cols, int tile_hint, cudaStream_t stream);
+
+// Columns per tile the launcher will use for K columns (for workspace sizing).
+template <typename S>
+int stripe_tile_width(int64_t K, int tile_hint, const void* X, const void* Y);
 
 }  // namespace gl

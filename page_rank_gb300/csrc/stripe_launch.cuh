@@ -6,38 +6,63 @@
 
 namespace gl {
 
-template <typename S, int BR, int V, int G, bool PPR>
+template <typename S, int BR, int V, int C, bool PPR>
 int launch_stripe_shape(const StripeArgs<S>& a0, cudaStream_t stream) {
     StripeArgs<S> a = a0;
-    constexpr int T = G * V;
+    constexpr int T = C * V;
     a.ntiles = (int)ceil_div(a.K, T);
-    const int64_t items = a.nstripes * a.batch * (int64_t)a.ntiles;
+    const int64_t units = (int64_t)a.num_pieces + a.nstripes;
+    const int64_t items = units * a.batch * (int64_t)a.ntiles;
     if (items == 0) return GL_OK;
-    auto kern = stripe_kernel<S, BR, BR, V, G, PPR>;
+    auto kern = stripe_kernel<S, BR, BR, V, C, PPR>;
+    constexpr size_t smem = stripe_smem_bytes<S, BR, V, C>();
     static int occ = 0;
     if (occ == 0) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int o = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, kStripeThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, kStripeThreads, smem);
         occ = o > 0 ? o : 1;
     }
-    const int64_t groups_per_block = (kStripeThreads / 32) * (32 / G);
-    int64_t blocks = ceil_div(items, groups_per_block);
+    int64_t blocks = ceil_div(items, kStripeWarps);
     const int64_t cap = (int64_t)num_sms() * occ;
     if (blocks > cap) blocks = cap;
-    kern<<<(unsigned)blocks, kStripeThreads, 0, stream>>>(a);
+    kern<<<(unsigned)blocks, kStripeThreads, smem, stream>>>(a);
     GL_LAUNCH_CHECK("stripe_kernel");
     return GL_OK;
 }
 
 inline bool aligned_to(const void* p, int bytes) { return (reinterpret_cast<uintptr_t>(p) % bytes) == 0; }
 
-// Widest vector the column count and both pointers allow.
+// Vector width and column lanes for K columns.  tile_hint (0 = automatic)
+// caps the tile width T = C * V, e.g. 64 instead of 128 for K = 256.
+struct Shape {
+    int V, C;
+};
+
 template <typename S>
-int pick_vec(const StripeArgs<S>& a, int want) {
-    int v = want;
-    while (v > 1 && (a.K % v != 0 || !aligned_to(a.X, v * (int)sizeof(S)) || !aligned_to(a.Y, v * (int)sizeof(S))))
-        v >>= 1;
-    return v;
+Shape pick_shape(int64_t K, int tile_hint, const void* X, const void* Y) {
+    auto vec_ok = [&](int v) {
+        return K % v == 0 && aligned_to(X, v * (int)sizeof(S)) && aligned_to(Y, v * (int)sizeof(S));
+    };
+    const int max_v = sizeof(S) == 4 ? 4 : 2;
+    int cap = tile_hint > 0 ? tile_hint : 1 << 30;
+    if (sizeof(S) == 8 && K < 17) return {1, 1};   // FP64 instantiates only C = 1 below 17 columns
+    if (K >= 32) {
+        for (int v = max_v; v >= 1; v >>= 1)
+            if (K >= 32 * v && 32 * v <= cap && vec_ok(v)) return {v, 32};
+        return {1, 32};
+    }
+    int c = 1;
+    while (c < K) c <<= 1;   // K <= 31 here: C = next power of two >= K, V = 1
+    if (c > 32) c = 32;
+    while (c > 1 && c > cap) c >>= 1;
+    return {1, c};
+}
+
+template <typename S>
+int stripe_tile_width(int64_t K, int tile_hint, const void* X, const void* Y) {
+    const Shape sh = pick_shape<S>(K, tile_hint, X, Y);
+    return sh.V * sh.C;
 }
 
 }  // namespace gl

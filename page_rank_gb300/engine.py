@@ -1,0 +1,262 @@
+"""Batched multi-seed Personalized PageRank on a resident graph.
+
+:class:`PPREngine` keeps one transition matrix resident in device memory as a
+PBR matrix and answers many personalization vectors at once: every query
+(a seed set, uniform weights) is one column of the iterate, so one fused
+kernel launch per iteration advances all of them (``gl_ppr_step``).
+
+Per-column retirement: columns whose L1 update falls below the tolerance are
+frozen by the kernel (STOP_PER_COLUMN) and, at chunk boundaries, removed from
+the working set — the still-active columns are gathered into a narrower
+iterate, so later iterations move fewer bytes.  Iteration chunks are captured
+once per working-set shape as CUDA graphs and replayed.
+
+Dangling nodes (sources without out-edges) send their mass to the teleport
+vector of each query (the missing-mass update of the reference's
+``batched_ppr_update_kernel``, ``kernels/ppr_kernel.cu:57-97``), so the matrix
+stays sparse (the reference's ``normalize_transition_matrix`` instead adds a
+dense 1/N column per dangling node, ``graph_link/__init__.py:200-206``).
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import scipy.sparse as sp
+import torch
+
+from . import native
+from .pbr import _ptr, pbr_from_device_csr
+from .ppr import PprRun, dangling_bitmap, teleport_from_seed_sets
+
+
+def certified_tolerance(tol: float, alpha: float) -> float:
+    """Update-size threshold that bounds the distance to the fixed point.
+
+    The iteration is an alpha-contraction in L1 on probability vectors, so
+    ||x_t - x*|| <= alpha / (1 - alpha) * ||x_t - x_{t-1}||; stopping when the
+    update is below tol * (1 - alpha) / alpha guarantees ||x_t - x*|| <= tol."""
+    return tol * (1.0 - alpha) / alpha
+
+
+@dataclass
+class BatchResult:
+    X: torch.Tensor                     # [n, K] final vectors, column k = query k
+    iterations: np.ndarray              # per column: iterations to convergence (-1 = not converged)
+    launched_iterations: int            # fused steps launched over the whole batch
+    converged: np.ndarray
+    seconds: float
+    column_steps: int = 0               # sum over launched steps of the working-set width
+    history: list = field(default_factory=list)
+
+
+class PPREngine:
+    """A transition matrix resident on one GPU, ready for batched PPR."""
+
+    def __init__(self, A: sp.csr_matrix, block_size: int = 8, min_nnz_per_block: int | None = None,
+                 device=None, dangling: np.ndarray | None = None, column_tile: int = 0):
+        if device is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        self.device = torch.device(device)
+        if A.shape[0] != A.shape[1]:
+            raise ValueError("transition matrix must be square")
+        if not A.has_canonical_format:
+            A = A.copy()
+            A.sum_duplicates()
+        self.n = A.shape[0]
+        self.block_size = int(block_size)
+        self.min_nnz = int(block_size if min_nnz_per_block is None else min_nnz_per_block)
+        with torch.cuda.device(self.device):
+            indptr = torch.from_numpy(A.indptr.astype(np.int32)).to(self.device)
+            indices = torch.from_numpy(A.indices.astype(np.int32)).to(self.device)
+            data = torch.from_numpy(A.data.astype(np.float32)).to(self.device)
+            self.pbr = pbr_from_device_csr(indptr, indices, data, self.n, self.n, self.block_size,
+                                           self.block_size, self.min_nnz)
+            self.mat = self.pbr.to(self.device)
+            from .graph_link.pbr_registry import get_pbr_gpu_meta
+            self.meta = get_pbr_gpu_meta(self.mat)
+            self.meta["column_tile"] = int(column_tile)
+            if dangling is None:
+                self.dbits = dangling_bitmap(indices, self.n)
+            else:
+                self.dbits = _bitmap_from_mask(np.asarray(dangling, bool), self.device)
+        self.nnz = int(A.nnz)
+        self._graphs: dict = {}
+
+    # -- sizes ----------------------------------------------------------------
+    def matrix_bytes(self) -> int:
+        m = self.meta
+        return int(sum(t.numel() * t.element_size() for k, t in m.items()))
+
+    def iteration_bytes(self, k: int) -> int:
+        """Algorithmic HBM bytes of one fused step with k columns: the matrix
+        structure once, X_t read once, X_{t+1} written once."""
+        nb = self.meta["codes"].numel()
+        packed = self.meta["data"].numel()
+        rem = self.meta["rem_col_ind"].numel()
+        return 20 * nb + 4 * packed + 4 * (self.n + 1) + 8 * rem + 8 * self.n * k
+
+    # -- queries --------------------------------------------------------------
+    def teleport(self, seed_sets) -> tuple:
+        ptr = np.zeros(len(seed_sets) + 1, dtype=np.int32)
+        ptr[1:] = np.cumsum([len(s) for s in seed_sets])
+        idx = np.concatenate([np.asarray(s, dtype=np.int32) for s in seed_sets]) if seed_sets else \
+            np.zeros(0, np.int32)
+        # duplicate seeds inside one set merge into one weighted entry so the
+        # kernel's epilogue sees unique (row, column) pairs
+        rows, cols, w = [], [], []
+        for k, s in enumerate(seed_sets):
+            u, c = np.unique(np.asarray(s, dtype=np.int64), return_counts=True)
+            rows.append(u)
+            cols.append(np.full(len(u), k))
+            w.append(c / c.sum())
+        if seed_sets:
+            rows = np.concatenate(rows).astype(np.int32)
+            w = np.concatenate(w).astype(np.float32)
+            ptr2 = np.zeros(len(seed_sets) + 1, dtype=np.int32)
+            ptr2[1:] = np.cumsum([len(np.unique(np.asarray(s))) for s in seed_sets])
+        else:
+            rows, w, ptr2 = idx, np.zeros(0, np.float32), ptr
+        dev = self.device
+        return (torch.from_numpy(ptr2).to(dev), torch.from_numpy(rows).to(dev),
+                torch.from_numpy(w).to(dev))
+
+    def solve(self, seed_sets, alpha: float = 0.85, tol: float = 1e-6, max_iterations: int = 1000,
+              certified: bool = True, retire: bool = True, chunk: int = 8, x0: torch.Tensor | None = None,
+              use_graphs: bool = True, compact_ratio: float = 0.75) -> BatchResult:
+        """Personalized PageRank for every seed set (one column each).
+
+        ``certified`` stops a column once its update is below
+        ``certified_tolerance(tol, alpha)`` so its distance to the exact fixed
+        point is at most ``tol`` in L1; otherwise the update itself is compared
+        with ``tol`` (the reference's rule)."""
+        K = len(seed_sets)
+        dev = self.device
+        thr = certified_tolerance(tol, alpha) if certified else tol
+        t0 = time.perf_counter()
+        with torch.cuda.device(dev):
+            ptr, rows, w = self.teleport(seed_sets)
+            out = torch.empty((self.n, K), dtype=torch.float32, device=dev)
+            col_iter = np.full(K, -1, dtype=np.int64)
+            active = np.arange(K)
+            cur_x0 = x0
+            done = 0
+            launched = 0
+            column_steps = 0
+            history = []
+            while active.size and done < max_iterations:
+                sub_ptr, sub_rows, sub_w = _select_columns(ptr, rows, w, active)
+                tp = teleport_from_seed_sets(sub_ptr, sub_rows, self.n, self.block_size, sub_w)
+                run = PprRun(self.meta, self.n, self.n, self.block_size, self.block_size, tp, alpha,
+                             max_iterations - done, thr,
+                             native.GL_PPR_STOP_PER_COLUMN if retire else native.GL_PPR_STOP_ALL,
+                             self.dbits)
+                run.init(cur_x0)
+                graph = None
+                steps = 0            # steps launched in this run
+                written = 0          # steps that wrote a new iterate
+                stop_all_at = None
+                fin = np.zeros(active.size, dtype=bool)
+                while steps < run.max_iterations:
+                    if use_graphs:
+                        if graph is None:
+                            graph = self._capture(run, chunk)
+                        graph.replay()
+                    else:
+                        run.launch_chunk(chunk)
+                    n_valid = min(chunk, run.max_iterations - steps)
+                    res = run.res_hist[steps:steps + n_valid].cpu().numpy()   # syncs
+                    for t in range(n_valid):
+                        row = res[t]
+                        history.append(float(row.max()))
+                        newly = (~fin) & (row < thr)
+                        col_iter[active[newly]] = done + steps + t + 1
+                        fin |= newly
+                        if not retire and (row < thr).all():
+                            stop_all_at = steps + t + 1
+                            break
+                    launched += n_valid if stop_all_at is None else stop_all_at - steps
+                    column_steps += (n_valid if stop_all_at is None else stop_all_at - steps) * active.size
+                    steps += n_valid
+                    written = steps if stop_all_at is None else stop_all_at
+                    if fin.all() or stop_all_at is not None:
+                        break
+                    if retire and fin.any() and fin.sum() >= (1.0 - compact_ratio) * active.size:
+                        break   # compact: restart with the still-active columns
+                Xcur = run.bufs[written % 2]
+                done += written
+                keep = ~fin if retire else np.zeros(active.size, dtype=bool)
+                if not retire or done >= max_iterations:
+                    keep_out = np.ones(active.size, dtype=bool)
+                else:
+                    keep_out = ~keep
+                sel = np.nonzero(keep_out)[0]
+                if sel.size:
+                    out[:, torch.from_numpy(active[sel]).to(dev)] = Xcur[:, torch.from_numpy(sel).to(dev)]
+                if retire and keep.any() and done < max_iterations:
+                    cur_x0 = Xcur[:, torch.from_numpy(np.nonzero(keep)[0]).to(dev)].contiguous()
+                    active = active[keep]
+                else:
+                    active = active[:0]
+            torch.cuda.synchronize(dev)
+        return BatchResult(X=out, iterations=col_iter, launched_iterations=launched,
+                           converged=col_iter >= 0, seconds=time.perf_counter() - t0,
+                           column_steps=column_steps, history=history)
+
+    def solve_plain(self, seed_sets, alpha: float = 0.85, tol: float = 1e-6, max_iterations: int = 1000,
+                    certified: bool = True) -> BatchResult:
+        """One query at a time (K = 1 per run): the plain GPU path batched
+        queries are compared against."""
+        K = len(seed_sets)
+        t0 = time.perf_counter()
+        out = torch.empty((self.n, K), dtype=torch.float32, device=self.device)
+        its = np.full(K, -1, dtype=np.int64)
+        launched = 0
+        for k, s in enumerate(seed_sets):
+            r = self.solve([s], alpha, tol, max_iterations, certified=certified, retire=False, chunk=8,
+                           use_graphs=False)
+            out[:, k] = r.X[:, 0]
+            its[k] = r.iterations[0]
+            launched += r.launched_iterations
+        torch.cuda.synchronize(self.device)
+        return BatchResult(X=out, iterations=its, launched_iterations=launched, converged=its >= 0,
+                           seconds=time.perf_counter() - t0, column_steps=launched)
+
+    def _capture(self, run: PprRun, chunk: int):
+        """CUDA graph of one chunk of steps for this run's buffers."""
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        # one eager chunk-sized warm call is not needed: the launcher's
+        # occupancy query happens outside capture on first use
+        _ = native.lib()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            run._warm_params(chunk)
+        with torch.cuda.graph(g, stream=s):
+            run.launch_chunk(chunk)
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        # capturing does not execute: the chunk counter is still at its base
+        return g
+
+
+def _select_columns(ptr: torch.Tensor, rows: torch.Tensor, w: torch.Tensor, active: np.ndarray):
+    p = ptr.cpu().numpy()
+    r = rows.cpu().numpy()
+    ww = w.cpu().numpy()
+    lens = p[active + 1] - p[active]
+    new_ptr = np.zeros(len(active) + 1, dtype=np.int32)
+    new_ptr[1:] = np.cumsum(lens)
+    idx = np.concatenate([np.arange(p[a], p[a + 1]) for a in active]) if len(active) else np.zeros(0, np.int64)
+    dev = ptr.device
+    return (torch.from_numpy(new_ptr).to(dev), torch.from_numpy(r[idx].astype(np.int32)).to(dev),
+            torch.from_numpy(ww[idx].astype(np.float32)).to(dev))
+
+
+def _bitmap_from_mask(mask: np.ndarray, device) -> torch.Tensor:
+    n = mask.size
+    words = max(1, -(-n // 32))
+    pad = np.zeros(words * 32, dtype=np.uint64)
+    pad[:n] = mask
+    packed = (pad.reshape(words, 32) << np.arange(32, dtype=np.uint64)).sum(axis=1).astype(np.uint32)
+    return torch.from_numpy(packed.view(np.int32)).to(device)

@@ -22,7 +22,8 @@ import torch
 
 from .. import native
 from ..pbr import (DataOrder, PBRMatrix, PBRMatrixInt32Double, PBRMatrixInt32Float,
-                   PBRMatrixInt64Double, PBRMatrixInt64Float, matrix_desc, pbr_from_device_csr)
+                   PBRMatrixInt64Double, PBRMatrixInt64Float, matrix_desc, pbr_from_device_csr,
+                   spmm_workspace)
 from ..ppr import PprRun, dangling_bitmap, teleport_from_seed_sets
 from .pbr_registry import clear_pbr_gpu_meta, get_pbr_gpu_meta, set_pbr_gpu_meta
 
@@ -60,10 +61,13 @@ def pbr_batched_matmul_cuda(pbr_mat, x: torch.Tensor) -> torch.Tensor:
     x3 = x3.contiguous()
     batch, _, width = x3.shape
     y = torch.empty((batch, pbr_mat.rows, width), dtype=x.dtype, device=x.device)
-    desc = matrix_desc(meta, pbr_mat.rows, pbr_mat.cols, pbr_mat.block_rows, pbr_mat.block_cols)
     with torch.cuda.device(x.device):
+        desc = matrix_desc(meta, pbr_mat.rows, pbr_mat.cols, pbr_mat.block_rows, pbr_mat.block_cols)
+        ws = spmm_workspace(meta, desc, batch, width, x.device)
         native.check(native.lib().gl_pbr_spmm(desc, x3.data_ptr() if x3.numel() else None,
                                               y.data_ptr() if y.numel() else None, batch, width,
+                                              ws.data_ptr() if ws is not None else None,
+                                              ws.numel() if ws is not None else 0,
                                               torch.cuda.current_stream(x.device).cuda_stream))
     return y
 

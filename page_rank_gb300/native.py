@@ -40,6 +40,7 @@ GL_ERR_WORKSPACE = 7
 GL_I32, GL_I64 = 0, 1
 GL_F32, GL_F64 = 0, 1
 GL_PPR_STOP_ALL, GL_PPR_STOP_PER_COLUMN = 0, 1
+GL_DANGLING_TO_TELEPORT, GL_DANGLING_UNIFORM = 0, 1
 
 
 def _nvcc() -> str:
@@ -120,7 +121,9 @@ class PbrMatrixDesc(_c.Structure):
                 ("value_type", _i32),
                 ("block_codes", _vp), ("block_coords", _vp), ("block_offsets", _vp),
                 ("block_data", _vp), ("remainder_indptr", _vp), ("remainder_col_ind", _vp),
-                ("remainder_data", _vp), ("stripe_block_ptr", _vp)]
+                ("remainder_data", _vp), ("stripe_block_ptr", _vp),
+                ("num_heavy", _i32), ("num_pieces", _i32), ("piece_work", _i32), ("column_tile", _i32),
+                ("heavy_of", _vp), ("heavy_stripe", _vp), ("heavy_first", _vp), ("piece_heavy", _vp)]
 
 
 class BuildCounts(_c.Structure):
@@ -136,7 +139,8 @@ class TeleportDesc(_c.Structure):
 class PprStepParams(_c.Structure):
     _fields_ = [("alpha", _c.c_double), ("tol", _c.c_double), ("stop_mode", _i32),
                 ("max_iterations", _i32), ("step_in_chunk", _i32), ("chunk_base", _vp),
-                ("residual_hist", _vp), ("dangling_hist", _vp), ("dangling_bitmap", _vp)]
+                ("residual_hist", _vp), ("dangling_hist", _vp), ("dangling_bitmap", _vp),
+                ("dangling_target", _i32)]
 
 
 # name -> (restype, argtypes)
@@ -150,13 +154,16 @@ _SIGS = {
                                      _i64, _c.POINTER(BuildCounts), _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                      _vp, _vp]),
     "gl_pbr_stripe_index": (_c.c_int, [_vp, _i64, _i64, _i32, _vp, _vp, _vp]),
-    "gl_pbr_spmm": (_c.c_int, [_c.POINTER(PbrMatrixDesc), _vp, _vp, _i64, _i64, _vp]),
+    "gl_pbr_schedule_elems": (_i64, [_c.POINTER(PbrMatrixDesc), _i32]),
+    "gl_pbr_schedule_build": (_c.c_int, [_c.POINTER(PbrMatrixDesc), _i32, _vp, _i64, _vp]),
+    "gl_pbr_spmm_workspace_bytes": (_i64, [_c.POINTER(PbrMatrixDesc), _i64, _i64]),
+    "gl_pbr_spmm": (_c.c_int, [_c.POINTER(PbrMatrixDesc), _vp, _vp, _i64, _i64, _vp, _i64, _vp]),
     "gl_ppr_teleport_index": (_c.c_int, [_i64, _i32, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp,
                                          _vp]),
     "gl_ppr_init": (_c.c_int, [_c.POINTER(TeleportDesc), _i64, _i64, _i32, _vp, _vp, _vp, _vp]),
     "gl_ppr_dangling_mass": (_c.c_int, [_vp, _i64, _i64, _i32, _vp, _vp, _vp]),
     "gl_ppr_step": (_c.c_int, [_c.POINTER(PbrMatrixDesc), _c.POINTER(TeleportDesc), _vp, _vp, _i64,
-                               _c.POINTER(PprStepParams), _vp]),
+                               _c.POINTER(PprStepParams), _vp, _i64, _vp]),
     "gl_counter_add": (_c.c_int, [_vp, _i32, _vp]),
 }
 

@@ -269,9 +269,14 @@ def pbr_from_device_csr(indptr: torch.Tensor, indices: torch.Tensor, data: torch
     return cls(rows, cols, block_rows, block_cols, int(indices.numel()), build)
 
 
+SCHED_FIELDS = ("num_heavy", "num_pieces", "piece_work", "heavy_of", "heavy_stripe", "heavy_first",
+                "piece_heavy")
+
+
 def matrix_desc(meta: dict, rows: int, cols: int, block_rows: int, block_cols: int
                 ) -> native.PbrMatrixDesc:
-    """C descriptor for a registered (int32-index) device matrix."""
+    """C descriptor for a registered (int32-index) device matrix, including its
+    load-balance schedule (built on first use and kept in ``meta``)."""
     d = native.PbrMatrixDesc()
     d.rows, d.cols = rows, cols
     d.block_rows, d.block_cols = block_rows, block_cols
@@ -287,4 +292,39 @@ def matrix_desc(meta: dict, rows: int, cols: int, block_rows: int, block_cols: i
     d.remainder_col_ind = _ptr(meta["rem_col_ind"])
     d.remainder_data = _ptr(meta["rem_vals"])
     d.stripe_block_ptr = _ptr(meta["stripe_ptr"])
+    d.column_tile = int(meta.get("column_tile", 0))
+    sched = meta.get("schedule")
+    if sched is None and block_rows == block_cols and block_rows in (2, 4, 8) and rows > 0:
+        sched = build_schedule(d, meta["stripe_ptr"].device, int(meta.get("piece_work", 0)))
+        meta["schedule"] = sched
+    if sched is not None:
+        for f in SCHED_FIELDS:
+            setattr(d, f, sched[f])
     return d
+
+
+def build_schedule(d: native.PbrMatrixDesc, device, piece_work: int = 0) -> dict:
+    L = native.lib()
+    elems = int(L.gl_pbr_schedule_elems(d, piece_work))
+    buf = torch.empty(max(elems, 1), dtype=torch.int32, device=device)
+    with torch.cuda.device(device):
+        native.check(L.gl_pbr_schedule_build(d, piece_work, buf.data_ptr(), elems,
+                                             torch.cuda.current_stream(device).cuda_stream))
+    sched = {f: getattr(d, f) for f in SCHED_FIELDS}
+    sched["buffer"] = buf          # keeps the device arrays alive
+    return sched
+
+
+def spmm_workspace(meta: dict, desc: native.PbrMatrixDesc, batch: int, K: int, device) -> torch.Tensor | None:
+    """Zero-filled workspace for gl_pbr_spmm / gl_ppr_step, cached per shape
+    and stream (a workspace must not be used by two launches at once)."""
+    nbytes = int(native.lib().gl_pbr_spmm_workspace_bytes(desc, batch, K))
+    if nbytes <= 0:
+        return None
+    key = (batch, K, torch.cuda.current_stream(device).cuda_stream)
+    cache = meta.setdefault("ws_cache", {})
+    ws = cache.get(key)
+    if ws is None or ws.numel() < nbytes:
+        ws = torch.zeros(nbytes, dtype=torch.uint8, device=device)
+        cache[key] = ws
+    return ws

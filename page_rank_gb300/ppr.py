@@ -98,7 +98,8 @@ class PprRun:
 
     def __init__(self, meta: dict, rows: int, cols: int, block_rows: int, block_cols: int,
                  teleport: Teleport, alpha: float, max_iterations: int, tol: float,
-                 stop_mode: int = native.GL_PPR_STOP_ALL, dangling_bits: torch.Tensor | None = None):
+                 stop_mode: int = native.GL_PPR_STOP_ALL, dangling_bits: torch.Tensor | None = None,
+                 dangling_target: int = native.GL_DANGLING_TO_TELEPORT):
         if rows != cols:
             raise ValueError("personalized PageRank needs a square matrix")
         self.meta = meta
@@ -111,6 +112,7 @@ class PprRun:
         self.tol = float(tol)
         self.stop_mode = stop_mode
         self.dangling_bits = dangling_bits
+        self.dangling_target = dangling_target
         dev = meta["data"].device
         dtype = meta["data"].dtype
         self.device = dev
@@ -120,6 +122,10 @@ class PprRun:
         self.dang_hist = torch.zeros((self.max_iterations + 1, self.K), dtype=torch.float64, device=dev)
         self.chunk_base = torch.zeros(1, dtype=torch.int32, device=dev)
         self._desc = matrix_desc(meta, rows, cols, block_rows, block_cols)
+        nbytes = int(native.lib().gl_pbr_spmm_workspace_bytes(self._desc, 1, self.K))
+        # owned by this run: a run's steps are stream-ordered, never concurrent
+        self.ws = torch.zeros(max(nbytes, 1), dtype=torch.uint8, device=dev)
+        self._ws_bytes = max(nbytes, 0)
         self._tpd = teleport.desc()
         self._vtype = native.GL_F32 if dtype == torch.float32 else native.GL_F64
         self._params = []
@@ -154,8 +160,25 @@ class PprRun:
             p.residual_hist = self.res_hist.data_ptr()
             p.dangling_hist = self.dang_hist.data_ptr()
             p.dangling_bitmap = _ptr(self.dangling_bits)
+            p.dangling_target = self.dangling_target
             self._params.append(p)
         return self._params[i]
+
+    def _warm_params(self, n: int) -> None:
+        """Create the step parameters for a chunk of n steps and make the
+        launcher run its one-time occupancy query with a step that returns at
+        once (iteration index past max_iterations), so that a following CUDA
+        graph capture records kernel launches only."""
+        for i in range(n):
+            self._step_params(i)
+        p = native.PprStepParams()
+        ctypes_copy = self._step_params(0)
+        for name, _ in native.PprStepParams._fields_:
+            setattr(p, name, getattr(ctypes_copy, name))
+        p.step_in_chunk = 1 << 30
+        native.check(native.lib().gl_ppr_step(self._desc, self._tpd, self.bufs[0].data_ptr(),
+                                              self.bufs[1].data_ptr(), self.K, p, self.ws.data_ptr(),
+                                              self._ws_bytes, self._stream()))
 
     def launch_chunk(self, n: int) -> None:
         """Launch n (even) steps starting at the device counter, then advance it."""
@@ -164,7 +187,7 @@ class PprRun:
         for i in range(n):
             native.check(L.gl_ppr_step(self._desc, self._tpd, self.bufs[i % 2].data_ptr(),
                                        self.bufs[(i + 1) % 2].data_ptr(), self.K,
-                                       self._step_params(i), st))
+                                       self._step_params(i), self.ws.data_ptr(), self._ws_bytes, st))
         native.check(L.gl_counter_add(self.chunk_base.data_ptr(), n, st))
 
     def run(self, chunk: int = 8, x0: torch.Tensor | None = None) -> PprResult:

@@ -119,7 +119,10 @@ def test_spmm_reference_uploaded_arrays(device):
     Xt = torch.from_numpy(X).to(device)
     Y = torch.empty(256, 32, device=device)
     desc = pbrmod.matrix_desc(meta, 256, 256, 4, 4)
+    ws = pbrmod.spmm_workspace(meta, desc, 1, 32, device)
     native.check(native.lib().gl_pbr_spmm(desc, Xt.data_ptr(), Y.data_ptr(), 1, 32,
+                                          ws.data_ptr() if ws is not None else None,
+                                          ws.numel() if ws is not None else 0,
                                           torch.cuda.current_stream().cuda_stream))
     _check(Y.cpu().numpy(), spmm_csr_fp64(A, X))
 
