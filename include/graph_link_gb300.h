@@ -266,6 +266,32 @@ int gl_ppr_step(const gl_pbr_matrix* A, const gl_teleport* tp,
  * that advances chunk_base at the end of a captured chunk of steps). */
 int gl_counter_add(int32_t* counter, int32_t delta, cudaStream_t stream);
 
+/* ======================================================================== */
+/* Learned warm start: 2-layer MLP kernels                                  */
+/* No counterpart in the reference.  f_in inputs (<= GL_MLP_MAX_IN) ->      */
+/* GL_MLP_HIDDEN ReLU units -> 1 output.  W1 [hidden][f_in] and w2 [hidden] */
+/* are BF16 (uint16 bit patterns); biases, inputs and accumulation FP32.    */
+/* ======================================================================== */
+#define GL_MLP_MAX_IN 16
+#define GL_MLP_HIDDEN 128
+
+/* out[e] = w2 . relu(W1 x_e + b1) + b2 for the n rows x_e of X [n][f_in]. */
+int gl_mlp_forward(const float* X, int64_t n, int32_t f_in, const uint16_t* W1, const float* b1,
+                   const uint16_t* w2, float b2, float* out, cudaStream_t stream);
+
+/* Gradient of sum_e (out_e - target_e)^2 / 2, added into grad
+ * ([W1 | b1 | w2 | b2] in FP32, hidden*f_in + 2*hidden + 1 entries; zero it
+ * first) and the loss added into *loss_sum (may be NULL). */
+int gl_mlp_backward(const float* X, const float* target, int64_t n, int32_t f_in, const uint16_t* W1,
+                    const float* b1, const uint16_t* w2, float b2, float* grad, double* loss_sum,
+                    cudaStream_t stream);
+
+/* One Adam step on the FP32 master parameters (same layout as grad, scaled
+ * by grad_scale first); refreshes the BF16 copies of W1 and w2.  step >= 1. */
+int gl_mlp_adam(float* params, const float* grad, float* m, float* v, int64_t count, float lr,
+                float beta1, float beta2, float eps, float grad_scale, int32_t step,
+                uint16_t* W1_bf16, uint16_t* w2_bf16, int32_t f_in, cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -111,146 +111,141 @@ __device__ __forceinline__ int32_t lower_bound_i32(const int32_t* offsets, int32
 }
 
 // ---------------------------------------------------------------------------
-// Asynchronous gather pipeline for P == 1 (one warp = one stripe, every lane
-// owns V columns).  The stripe's work is a sequence of "groups": one group per
-// PBR block (the X rows of its active columns) followed by groups of
-// kRemGroup remainder entries.  Each group's X-row pieces are copied global
-// -> shared with cp.async (LDGSTS, one 4/8/16-byte copy per lane per row)
-// into the lane's own slots of pipeline stage g % stages; kStages groups are
-// in flight while the oldest is consumed.  cp.async.wait_group is a hardware
-// wait (no software spin).  Each lane reads back only its own slots, so no
-// barrier is needed between lanes.
+// Accumulation for P == 1 (one warp = one stripe, every lane owns V columns),
+// in two phases per stripe row:
+//   decode  — lanes take one block each (32 blocks per pass, metadata in
+//             registers), extract the block's bits of row r, and write their
+//             (column, value) entries to the warp's list in shared memory at
+//             slots given by a warp prefix sum; the row's remainder entries
+//             are appended lane-parallel after them;
+//   consume — the whole warp walks the row's list: one broadcast shared load
+//             per entry, the X-row gathers issued eight at a time before their
+//             FMAs, accumulators of row r addressed statically.
+// Decoding is lane-parallel (a few instructions per nonzero spread over the
+// warp); consuming costs one load, one address and V FMAs per nonzero.
 // ---------------------------------------------------------------------------
-constexpr int kRemGroup = 8;
+constexpr int kListCap = 512;     // entries per warp list (>= 32 blocks x 8 bits)
+// row gathers in flight per warp: enough bytes in flight per SM at moderate
+// register cost (V = 4 moves 512 B per gather)
 template <int V>
-struct PipeCfg {
-    static constexpr int kStages = V >= 4 ? 2 : 3;
-    static constexpr int kSlots = 8;   // max(block columns, kRemGroup)
+struct Gather {
+    static constexpr int n = V >= 4 ? 4 : 8;
 };
 
-template <int BYTES>
-__device__ __forceinline__ void cp_async_lane(void* smem, const void* gmem) {
-    const unsigned dst = static_cast<unsigned>(__cvta_generic_to_shared(smem));
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(dst), "l"(gmem), "n"(BYTES) : "memory");
+// The list is padded to a multiple of the gather depth with (column 0,
+// value 0) entries, so the loop carries no predicates; lanes past the last
+// column gather from a clamped (valid) address and never store.
+template <typename S, int V>
+__device__ __forceinline__ void consume_list(S (&t)[V], const int32_t* lcol, const S* lval, int n_padded,
+                                             const S* __restrict__ Xb, int32_t K) {
+    constexpr int NG = Gather<V>::n;
+    for (int e0 = 0; e0 < n_padded; e0 += NG) {
+        Pack<S, V> x[NG];
+#pragma unroll
+        for (int q = 0; q < NG; ++q) x[q] = load_pack<S, V>(Xb + (long long)lcol[e0 + q] * K);
+#pragma unroll
+        for (int q = 0; q < NG; ++q) {
+            const S v = lval[e0 + q];
+#pragma unroll
+            for (int j = 0; j < V; ++j) t[j] = fma(v, x[q].v[j], t[j]);
+        }
+    }
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Pads the list [0, n) with (0, 0) entries up to a multiple of the gather
+// depth (never past kListCap, which is a multiple of it); returns the padded length.
+template <typename S, int V>
+__device__ __forceinline__ int pad_list(int32_t* lcol, S* lval, int n, int lane) {
+    constexpr int NG = Gather<V>::n;
+    const int np = (n + NG - 1) / NG * NG;
+    if (lane < np - n) {
+        lcol[n + lane] = 0;
+        lval[n + lane] = S(0);
+    }
+    __syncwarp();
+    return np;
+}
 
 template <typename S, int BR, int BC, int V>
-__device__ __forceinline__ void accumulate_pipelined(const StripeArgs<S>& a, S (&acc)[BR][V], unsigned char* xs_raw,
-                                                     int64_t s, int32_t b0, int32_t b1, int32_t j0, int32_t j1,
-                                                     const S* __restrict__ Xb, bool lane_ok, int lane) {
-    constexpr int ST = PipeCfg<V>::kStages;
-    constexpr int SL = PipeCfg<V>::kSlots;
-    constexpr int BYTES = V * (int)sizeof(S);
+__device__ __forceinline__ void accumulate_lists(const StripeArgs<S>& a, S (&acc)[BR][V], unsigned char* smem_raw,
+                                                 int64_t s, int32_t b0, int32_t b1, int32_t j0, int32_t j1,
+                                                 const S* __restrict__ Xb, bool lane_ok, int lane) {
     constexpr uint32_t ROWMASK = (BC >= 32) ? 0xffffffffu : ((1u << BC) - 1u);
-    Pack<S, V>* xs = reinterpret_cast<Pack<S, V>*>(xs_raw);
-    auto slot = [&](int stage, int k) -> Pack<S, V>* {
-        return xs + ((size_t)(stage * SL + k) * kStripeThreads + threadIdx.x);
-    };
-    // end of each stripe row inside the remainder range, for entry -> row
-    int32_t row_end[BR];
-#pragma unroll
-    for (int r = 0; r < BR; ++r) {
-        const int64_t row = s * BR + r;
-        row_end[r] = (row < a.rows) ? a.rem_ptr[row + 1] : j1;
-    }
-    const int32_t n_rem_groups = (j1 - j0 + kRemGroup - 1) / kRemGroup;
+    const int warp = threadIdx.x >> 5;
+    int32_t* lcol = reinterpret_cast<int32_t*>(smem_raw) + warp * kListCap;
+    S* lval = reinterpret_cast<S*>(smem_raw + (size_t)kStripeWarps * kListCap * sizeof(int32_t)) + warp * kListCap;
 
     for (int32_t kc = b0; kc < b1 || kc == b0; kc += 32) {
-        // blocks of this 32-chunk (metadata in lane registers), plus the
-        // remainder groups when this is the last chunk
         const int32_t nb = (b1 - kc) < 32 ? (b1 - kc > 0 ? b1 - kc : 0) : 32;
-        const bool last_chunk = kc + 32 >= b1;
-        uint64_t m_code = 0;
-        int32_t m_col = 0, m_off = 0;
+        const bool last = kc + 32 >= b1;
+        uint64_t code = 0;
+        int32_t col0 = 0, off = 0;
         if (lane < nb) {
-            m_code = static_cast<uint64_t>(a.codes[kc + lane]);
-            m_col = a.coords[2 * (int64_t)(kc + lane) + 1];
-            m_off = a.offsets[kc + lane];
+            code = static_cast<uint64_t>(a.codes[kc + lane]);
+            col0 = a.coords[2 * (int64_t)(kc + lane) + 1];
+            off = a.offsets[kc + lane];
         }
-        const int32_t ng = nb + (last_chunk ? n_rem_groups : 0);
-
-        auto issue = [&](int32_t g) {
-            if (g < ng) {                       // warp-uniform
-                const int stage = g % ST;
-                if (g < nb) {
-                    const uint64_t code = __shfl_sync(0xffffffffu, m_code, g);
-                    const int64_t col0 = __shfl_sync(0xffffffffu, m_col, g);
-                    if (lane_ok) {
-                        uint32_t colmask = 0;
+#pragma unroll 1
+        for (int r = 0; r < BR; ++r) {
+            // accumulators of row r, moved to a statically indexed temporary
+            S t[V];
 #pragma unroll
-                        for (int r = 0; r < BR; ++r) colmask |= (uint32_t)(code >> (r * BC)) & ROWMASK;
+            for (int j = 0; j < V; ++j) t[j] = S(0);
 #pragma unroll
-                        for (int c = 0; c < BC; ++c)
-                            if ((colmask >> c) & 1u) cp_async_lane<BYTES>(slot(stage, c), Xb + (col0 + c) * a.K);
-                    }
-                } else if (lane_ok) {
-                    const int32_t jg = j0 + (g - nb) * kRemGroup;
-                    const int32_t cnt = (j1 - jg) < kRemGroup ? (j1 - jg) : kRemGroup;
+            for (int rr = 0; rr < BR; ++rr)
+                if (rr == r) {
 #pragma unroll
-                    for (int q = 0; q < kRemGroup; ++q)
-                        if (q < cnt) cp_async_lane<BYTES>(slot(stage, q), Xb + (int64_t)a.rem_col[jg + q] * a.K);
+                    for (int j = 0; j < V; ++j) t[j] = acc[rr][j];
+                }
+            // ---- decode the chunk's bits of row r into the list -------------
+            uint32_t rb = (uint32_t)(code >> (r * BC)) & ROWMASK;
+            const int cnt = __popc(rb);
+            int pos = (int)warp_incl_scan_i64(cnt) - cnt;
+            const int nblk = __shfl_sync(0xffffffffu, pos + cnt, 31);
+            if (rb) {
+                int32_t k = off + (r == 0 ? 0 : __popcll(code & ((1ull << (r * BC)) - 1ull)));
+                while (rb) {
+                    const int c = __ffs(rb) - 1;
+                    rb &= rb - 1u;
+                    lcol[pos] = col0 + c;
+                    lval[pos] = a.bdata[k++];
+                    ++pos;
                 }
             }
-            cp_async_commit();
-        };
-
-#pragma unroll
-        for (int g = 0; g < ST - 1; ++g) issue(g);
-        for (int32_t g = 0; g < ng; ++g) {
-            issue(g + ST - 1);
-            cp_async_wait<ST - 1>();
-            const int stage = g % ST;
-            if (g < nb) {
-                const uint64_t code = __shfl_sync(0xffffffffu, m_code, g);
-                int32_t k = __shfl_sync(0xffffffffu, m_off, g);
-#pragma unroll
-                for (int r = 0; r < BR; ++r) {
-                    uint32_t bits = (uint32_t)(code >> (r * BC)) & ROWMASK;
-                    while (bits) {
-                        const int c = __ffs(bits) - 1;
-                        bits &= bits - 1u;
-                        const S v = a.bdata[k++];
-                        if (lane_ok) {
-                            const Pack<S, V> x = *slot(stage, c);
-#pragma unroll
-                            for (int j = 0; j < V; ++j) acc[r][j] = fma(v, x.v[j], acc[r][j]);
-                        }
+            int n = nblk;
+            // ---- append the row's remainder entries (last chunk only) ----------
+            const int64_t row = s * BR + r;
+            if (last && row < a.rows) {
+                int32_t rs = a.rem_ptr[row], re = a.rem_ptr[row + 1];
+                rs = rs > j0 ? rs : j0;
+                re = re < j1 ? re : j1;
+                while (rs < re) {
+                    const int room = kListCap - Gather<V>::n - n;
+                    const int take = (re - rs) < room ? (re - rs) : room;
+                    for (int q = lane; q < take; q += 32) {
+                        lcol[n + q] = a.rem_col[rs + q];
+                        lval[n + q] = a.rem_val[rs + q];
                     }
-                }
-            } else {
-                const int32_t jg = j0 + (g - nb) * kRemGroup;
-                const int32_t cnt = (j1 - jg) < kRemGroup ? (j1 - jg) : kRemGroup;
-                // lane q < cnt fetches value and row of entry jg + q
-                S my_v = S(0);
-                int my_r = 0;
-                if (lane < cnt) {
-                    const int32_t j = jg + lane;
-                    my_v = a.rem_val[j];
-#pragma unroll
-                    for (int r = 0; r < BR - 1; ++r) my_r += (j >= row_end[r]) ? 1 : 0;
-                }
-#pragma unroll
-                for (int q = 0; q < kRemGroup; ++q) {
-                    if (q < cnt) {
-                        const S v = __shfl_sync(0xffffffffu, my_v, q);
-                        const int rq = __shfl_sync(0xffffffffu, my_r, q);
-                        if (lane_ok) {
-                            const Pack<S, V> x = *slot(stage, q);
-#pragma unroll
-                            for (int r = 0; r < BR; ++r)
-                                if (r == rq) {
-#pragma unroll
-                                    for (int j = 0; j < V; ++j) acc[r][j] = fma(v, x.v[j], acc[r][j]);
-                                }
-                        }
+                    __syncwarp();
+                    n += take;
+                    rs += take;
+                    if (rs < re) {   // list full: consume and continue
+                        consume_list<S, V>(t, lcol, lval, pad_list<S, V>(lcol, lval, n, lane), Xb, a.K);
+                        __syncwarp();
+                        n = 0;
                     }
                 }
             }
+            __syncwarp();
+            consume_list<S, V>(t, lcol, lval, pad_list<S, V>(lcol, lval, n, lane), Xb, a.K);
+            __syncwarp();
+#pragma unroll
+            for (int rr = 0; rr < BR; ++rr)
+                if (rr == r) {
+#pragma unroll
+                    for (int j = 0; j < V; ++j) acc[rr][j] = t[j];
+                }
         }
-        cp_async_wait<0>();
         if (kc >= b1) break;   // empty block range: one pass for the remainder
     }
 }
@@ -258,12 +253,18 @@ __device__ __forceinline__ void accumulate_pipelined(const StripeArgs<S>& a, S (
 // Dynamic shared memory of one CTA of stripe_kernel.
 template <typename S, int BC, int V, int C>
 constexpr size_t stripe_smem_bytes() {
-    return (32 / C == 1) ? (size_t)PipeCfg<V>::kStages * PipeCfg<V>::kSlots * kStripeThreads * V * sizeof(S)
+    return (32 / C == 1) ? (size_t)kStripeWarps * kListCap * (sizeof(int32_t) + sizeof(S))
                          : (size_t)BC * kStripeThreads * V * sizeof(S);
 }
 
+// Minimum resident CTAs per SM the register allocation must allow.
+template <int V>
+struct MinBlocks {
+    static constexpr int n = V >= 4 ? 2 : 3;
+};
+
 template <typename S, int BR, int BC, int V, int C, bool PPR>
-__global__ void __launch_bounds__(kStripeThreads)
+__global__ void __launch_bounds__(kStripeThreads, MinBlocks<V>::n)
 stripe_kernel(const StripeArgs<S> a) {
     constexpr int P = 32 / C;            // nonzero lanes per warp
     constexpr int T = C * V;             // columns per tile
@@ -407,10 +408,11 @@ stripe_kernel(const StripeArgs<S> a) {
 #pragma unroll
             for (int j = 0; j < V; ++j) acc[r][j] = S(0);
 
-        const S* __restrict__ Xb = a.X + b * a.cols * (int64_t)a.K + col_base;
+        // lanes past the last column read a valid address and never store
+        const S* __restrict__ Xb = a.X + b * a.cols * (int64_t)a.K + (lane_ok ? col_base : 0);
 
         if constexpr (P == 1) {
-            accumulate_pipelined<S, BR, BC, V>(a, acc, xs_dyn, s, b0, b1, j0, j1, Xb, lane_ok, lane);
+            accumulate_lists<S, BR, BC, V>(a, acc, xs_dyn, s, b0, b1, j0, j1, Xb, lane_ok, lane);
         } else {
             // ---- PBR blocks: lanes stride the blocks ------------------------
             for (int32_t kb = b0 + p_lane; kb < b1; kb += P) {

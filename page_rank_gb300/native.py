@@ -41,6 +41,7 @@ GL_I32, GL_I64 = 0, 1
 GL_F32, GL_F64 = 0, 1
 GL_PPR_STOP_ALL, GL_PPR_STOP_PER_COLUMN = 0, 1
 GL_DANGLING_TO_TELEPORT, GL_DANGLING_UNIFORM = 0, 1
+GL_MLP_MAX_IN, GL_MLP_HIDDEN = 16, 128
 
 
 def _nvcc() -> str:
@@ -165,6 +166,10 @@ _SIGS = {
     "gl_ppr_step": (_c.c_int, [_c.POINTER(PbrMatrixDesc), _c.POINTER(TeleportDesc), _vp, _vp, _i64,
                                _c.POINTER(PprStepParams), _vp, _i64, _vp]),
     "gl_counter_add": (_c.c_int, [_vp, _i32, _vp]),
+    "gl_mlp_forward": (_c.c_int, [_vp, _i64, _i32, _vp, _vp, _vp, _c.c_float, _vp, _vp]),
+    "gl_mlp_backward": (_c.c_int, [_vp, _vp, _i64, _i32, _vp, _vp, _vp, _c.c_float, _vp, _vp, _vp]),
+    "gl_mlp_adam": (_c.c_int, [_vp, _vp, _vp, _vp, _i64, _c.c_float, _c.c_float, _c.c_float, _c.c_float,
+                               _c.c_float, _i32, _vp, _vp, _i32, _vp]),
 }
 
 

@@ -1,0 +1,264 @@
+"""Learned warm start for batched PPR.
+
+A 2-layer MLP (10 inputs -> 128 ReLU -> 1; BF16 weight matrices, FP32
+accumulation; trained and run by this library's own kernels
+``gl_mlp_forward / gl_mlp_backward / gl_mlp_adam``) predicts log-PPR of every
+(node, query) pair from per-node features:
+
+  log(1 + in-degree), log(1 + out-degree),
+  one-hot hop distance to the nearest seed (0, 1, 2, 3, 4, farther),
+  log of the 1-step and 2-step propagated seed mass (A v, A^2 v).
+
+The features come from the fused SpMM (``gl_pbr_spmm``) applied to the seed
+vectors and to reachability indicators.  The prediction, exponentiated and
+normalized per column, starts the power iteration; the iteration then runs
+to the same tolerance, so the fixed point and its accuracy do not depend on
+the network.  A column whose first-step residual from the predicted start is
+larger than from the cold start (the teleport vector) falls back to the cold
+start.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import native
+from .engine import PPREngine
+from .pbr import _ptr, matrix_desc, spmm_workspace
+from .ppr import PprRun, teleport_from_seed_sets
+
+F_IN = 10
+HIDDEN = native.GL_MLP_HIDDEN
+N_PARAMS = HIDDEN * F_IN + 2 * HIDDEN + 1
+LOG_FLOOR = 1e-10
+
+
+class MLP:
+    """Parameters and optimizer state of the warm-start network (device)."""
+
+    def __init__(self, device, seed: int = 0):
+        g = torch.Generator().manual_seed(seed)
+        p = torch.zeros(N_PARAMS, dtype=torch.float32)
+        bound1 = 1.0 / math.sqrt(F_IN)
+        p[: HIDDEN * F_IN] = (torch.rand(HIDDEN * F_IN, generator=g) * 2 - 1) * bound1
+        p[HIDDEN * F_IN: HIDDEN * F_IN + HIDDEN] = 0.01
+        bound2 = 1.0 / math.sqrt(HIDDEN)
+        p[HIDDEN * F_IN + HIDDEN: HIDDEN * F_IN + 2 * HIDDEN] = (torch.rand(HIDDEN, generator=g) * 2 - 1) * bound2
+        p[-1] = math.log(1e-7)
+        self.device = device
+        self.params = p.to(device)
+        self.m = torch.zeros_like(self.params)
+        self.v = torch.zeros_like(self.params)
+        self.grad = torch.zeros_like(self.params)
+        self.W1 = torch.zeros(HIDDEN * F_IN, dtype=torch.int16, device=device)
+        self.w2 = torch.zeros(HIDDEN, dtype=torch.int16, device=device)
+        self.loss = torch.zeros(1, dtype=torch.float64, device=device)
+        self.step = 0
+        self._refresh_bf16()
+
+    def _refresh_bf16(self):
+        # round-to-nearest-even BF16 copies of the FP32 master weights
+        def to_bf16_bits(t):
+            u = t.contiguous().view(torch.int32).to(torch.int64) & 0xFFFFFFFF
+            lsb = (u >> 16) & 1
+            r = (u + 0x7FFF + lsb) >> 16
+            return (r & 0xFFFF).to(torch.int32).to(torch.int16)
+        self.W1.copy_(to_bf16_bits(self.params[: HIDDEN * F_IN]))
+        self.w2.copy_(to_bf16_bits(self.params[HIDDEN * F_IN + HIDDEN: HIDDEN * F_IN + 2 * HIDDEN]))
+
+    @property
+    def b1(self) -> torch.Tensor:
+        return self.params[HIDDEN * F_IN: HIDDEN * F_IN + HIDDEN]
+
+    def b2(self) -> float:
+        return float(self.params[-1].item())
+
+    def forward(self, X: torch.Tensor, b2: float | None = None) -> torch.Tensor:
+        X = X.contiguous()
+        out = torch.empty(X.shape[0], dtype=torch.float32, device=self.device)
+        native.check(native.lib().gl_mlp_forward(
+            _ptr(X), X.shape[0], F_IN, self.W1.data_ptr(), self.b1.data_ptr(), self.w2.data_ptr(),
+            self.b2() if b2 is None else b2, _ptr(out), torch.cuda.current_stream(self.device).cuda_stream))
+        return out
+
+    def gradient(self, X: torch.Tensor, target: torch.Tensor) -> tuple[torch.Tensor, float]:
+        self.grad.zero_()
+        self.loss.zero_()
+        native.check(native.lib().gl_mlp_backward(
+            _ptr(X.contiguous()), _ptr(target.contiguous()), X.shape[0], F_IN, self.W1.data_ptr(),
+            self.b1.data_ptr(), self.w2.data_ptr(), self.b2(), self.grad.data_ptr(), self.loss.data_ptr(),
+            torch.cuda.current_stream(self.device).cuda_stream))
+        return self.grad, float(self.loss.item())
+
+    def adam_step(self, n_examples: int, lr: float = 2e-3):
+        self.step += 1
+        native.check(native.lib().gl_mlp_adam(
+            self.params.data_ptr(), self.grad.data_ptr(), self.m.data_ptr(), self.v.data_ptr(), N_PARAMS,
+            lr, 0.9, 0.999, 1e-8, 1.0 / max(1, n_examples), self.step, self.W1.data_ptr(),
+            self.w2.data_ptr(), F_IN, torch.cuda.current_stream(self.device).cuda_stream))
+
+
+@dataclass
+class TrainStats:
+    vectors: int
+    examples: int
+    seconds: float
+    losses: list = field(default_factory=list)
+
+
+class WarmStart:
+    """Feature extraction, training and warm-started solves for one engine."""
+
+    def __init__(self, engine: PPREngine, seed: int = 0):
+        self.eng = engine
+        self.dev = engine.device
+        self.mlp = MLP(self.dev, seed)
+        n = engine.n
+        indptr = engine.pbr._build.rem_indptr  # placeholder to keep device; degrees below
+        A_rows = torch.as_tensor(np.diff(engine.host_indptr), device=self.dev, dtype=torch.float32)
+        out_deg = torch.bincount(torch.as_tensor(engine.host_indices, device=self.dev, dtype=torch.int64),
+                                 minlength=n).to(torch.float32)
+        self.log_in = torch.log1p(A_rows)
+        self.log_out = torch.log1p(out_deg)
+        self._desc = matrix_desc(engine.meta, n, n, engine.block_size, engine.block_size)
+        del indptr
+
+    # -- features -------------------------------------------------------------
+    def _spmm(self, X: torch.Tensor) -> torch.Tensor:
+        K = X.shape[1]
+        Y = torch.empty_like(X)
+        ws = spmm_workspace(self.eng.meta, self._desc, 1, K, self.dev)
+        native.check(native.lib().gl_pbr_spmm(self._desc, X.data_ptr(), Y.data_ptr(), 1, K,
+                                              ws.data_ptr() if ws is not None else None,
+                                              ws.numel() if ws is not None else 0,
+                                              torch.cuda.current_stream(self.dev).cuda_stream))
+        return Y
+
+    def seed_matrix(self, seed_sets) -> torch.Tensor:
+        ptr, rows, w = self.eng.teleport(seed_sets)
+        tp = teleport_from_seed_sets(ptr, rows, self.eng.n, self.eng.block_size, w)
+        V = torch.empty((self.eng.n, len(seed_sets)), dtype=torch.float32, device=self.dev)
+        native.check(native.lib().gl_ppr_init(tp.desc(), self.eng.n, len(seed_sets), native.GL_F32,
+                                              V.data_ptr(), None, None,
+                                              torch.cuda.current_stream(self.dev).cuda_stream))
+        return V
+
+    def raw_features(self, V: torch.Tensor):
+        """(m1, m2, hop) for the columns of V; hop in 0..5 (5 = farther than 4)."""
+        m1 = self._spmm(V)
+        m2 = self._spmm(m1)
+        reach = V > 0
+        hop = torch.full(V.shape, 5, dtype=torch.uint8, device=self.dev)
+        hop[reach] = 0
+        r1 = (m1 > 0) & ~reach
+        hop[r1] = 1
+        reach |= r1
+        r2 = (m2 > 0) & ~reach
+        hop[r2] = 2
+        reach |= r2
+        frontier = reach.to(torch.float32)
+        for h in (3, 4):
+            nxt = (self._spmm(frontier) > 0) & ~reach
+            hop[nxt] = h
+            reach |= nxt
+            frontier = reach.to(torch.float32)
+        return m1, m2, hop
+
+    def assemble(self, rows: torch.Tensor, m1: torch.Tensor, m2: torch.Tensor, hop: torch.Tensor) -> torch.Tensor:
+        """Feature rows for nodes `rows` (1-D) of one column's m1/m2/hop (1-D)."""
+        f = torch.empty((rows.numel(), F_IN), dtype=torch.float32, device=self.dev)
+        f[:, 0] = self.log_in[rows]
+        f[:, 1] = self.log_out[rows]
+        oh = torch.nn.functional.one_hot(hop.long(), 6).to(torch.float32)
+        f[:, 2:8] = oh
+        f[:, 8] = torch.log(m1 + LOG_FLOOR) / 10.0
+        f[:, 9] = torch.log(m2 + LOG_FLOOR) / 10.0
+        return f
+
+    # -- training ---------------------------------------------------------------
+    def train(self, num_vectors: int = 20000, batch: int = 256, nodes_per_vector: int = 512,
+              alpha: float = 0.85, tol: float = 1e-6, lr: float = 2e-3, minibatch: int = 65536,
+              epochs: int = 2, seed: int = 100) -> TrainStats:
+        """Solve num_vectors seed sets (sizes 1-32) with the plain method (the
+        engine without warm start) and fit the network to their log-PPR on
+        sampled nodes (most by PPR mass, some uniform)."""
+        from . import synth
+        t0 = time.perf_counter()
+        gen = torch.Generator(device=self.dev).manual_seed(seed)
+        feats, targs = [], []
+        done = 0
+        while done < num_vectors:
+            k = min(batch, num_vectors - done)
+            sets = synth.seed_sets(self.eng.n, k, 1, 32, seed=seed + done)
+            res = self.eng.solve(sets, alpha=alpha, tol=tol)
+            V = self.seed_matrix(sets)
+            m1, m2, hop = self.raw_features(V)
+            X = res.X.clamp_min(0)
+            n_mass = nodes_per_vector * 3 // 4
+            n_uni = nodes_per_vector - n_mass
+            idx_mass = torch.multinomial(X.T + 1e-30, n_mass, replacement=True, generator=gen)   # [k, n_mass]
+            idx_uni = torch.randint(0, self.eng.n, (k, n_uni), device=self.dev, generator=gen)
+            idx = torch.cat([idx_mass, idx_uni], dim=1)                                          # [k, S]
+            cols = torch.arange(k, device=self.dev)[:, None].expand_as(idx)
+            rows = idx.reshape(-1)
+            cc = cols.reshape(-1)
+            f = self.assemble(rows, m1[rows, cc], m2[rows, cc], hop[rows, cc])
+            feats.append(f)
+            targs.append(torch.log(X[rows, cc] + LOG_FLOOR))
+            done += k
+        Xf = torch.cat(feats)
+        T = torch.cat(targs)
+        n = Xf.shape[0]
+        losses = []
+        for _ in range(epochs):
+            perm = torch.randperm(n, device=self.dev, generator=gen)
+            for s0 in range(0, n, minibatch):
+                sel = perm[s0:s0 + minibatch]
+                _, loss = self.mlp.gradient(Xf[sel], T[sel])
+                self.mlp.adam_step(sel.numel(), lr)
+                losses.append(loss / sel.numel())
+        torch.cuda.synchronize(self.dev)
+        return TrainStats(vectors=num_vectors, examples=n, seconds=time.perf_counter() - t0, losses=losses)
+
+    # -- inference ----------------------------------------------------------------
+    def predict(self, seed_sets, chunk: int = 32) -> torch.Tensor:
+        """Predicted start vectors [n, K] (each column sums to 1)."""
+        n = self.eng.n
+        out = torch.empty((n, len(seed_sets)), dtype=torch.float32, device=self.dev)
+        all_rows = torch.arange(n, device=self.dev)
+        for c0 in range(0, len(seed_sets), chunk):
+            sets = seed_sets[c0:c0 + chunk]
+            V = self.seed_matrix(sets)
+            m1, m2, hop = self.raw_features(V)
+            for k in range(len(sets)):
+                f = self.assemble(all_rows, m1[:, k], m2[:, k], hop[:, k])
+                y = self.mlp.forward(f)
+                x = torch.exp(y - y.max())
+                out[:, c0 + k] = x / x.sum()
+        return out
+
+    def solve(self, seed_sets, alpha: float = 0.85, tol: float = 1e-6, max_iterations: int = 1000, **kw):
+        """Warm-started batched solve with per-column fallback to the cold start."""
+        x_warm = self.predict(seed_sets)
+        V = self.seed_matrix(seed_sets)
+        r_warm = self.first_residual(seed_sets, x_warm, alpha)
+        r_cold = self.first_residual(seed_sets, V, alpha)
+        use_warm = r_warm < r_cold
+        x0 = torch.where(torch.from_numpy(use_warm).to(self.dev)[None, :], x_warm, V)
+        res = self.eng.solve(seed_sets, alpha=alpha, tol=tol, max_iterations=max_iterations, x0=x0, **kw)
+        res.warm_columns = use_warm
+        return res
+
+    def first_residual(self, seed_sets, x0: torch.Tensor, alpha: float) -> np.ndarray:
+        """||P(x0) - x0||_1 per column (one fused step)."""
+        ptr, rows, w = self.eng.teleport(seed_sets)
+        tp = teleport_from_seed_sets(ptr, rows, self.eng.n, self.eng.block_size, w)
+        run = PprRun(self.eng.meta, self.eng.n, self.eng.n, self.eng.block_size, self.eng.block_size, tp,
+                     alpha, 2, 0.0, native.GL_PPR_STOP_ALL, self.eng.dbits)
+        run.init(x0)
+        run.launch_chunk(2)
+        return run.res_hist[0].cpu().numpy()
