@@ -165,6 +165,22 @@ int gl_pbr_spmm(const gl_pbr_matrix* A, const void* X, void* Y,
                 int64_t batch, int64_t features, void* workspace, int64_t workspace_bytes,
                 cudaStream_t stream);
 
+/* gl_pbr_spmm for callers that cannot allocate device memory when they call
+ * it (a host program whose device memory is all owned by its own allocator,
+ * or a latency-critical loop that must not wait on cudaMalloc / cudaFree).
+ * No counterpart in the reference.  Same arguments and result as gl_pbr_spmm
+ * without the workspace: the scratch lives in a static device array of
+ * GL_SPMM_STATIC_SCRATCH_BYTES that every GPU loading this library holds
+ * until exit.  Calls needing more scratch than that (see
+ * gl_pbr_spmm_workspace_bytes) fail with GL_ERR_WORKSPACE before launching.
+ * All calls on a device share the array, so calls that overlap on the GPU
+ * race; the array keeps the last call's contents (the call clears what must
+ * start at zero).  The first call on a device looks up the array's address
+ * with cudaGetSymbolAddress, so make it before any stream capture. */
+#define GL_SPMM_STATIC_SCRATCH_BYTES (16u * 1024u * 1024u)
+int gl_pbr_spmm_static(const gl_pbr_matrix* A, const void* X, void* Y,
+                       int64_t batch, int64_t features, cudaStream_t stream);
+
 /* ======================================================================== */
 /* Personalized PageRank                                                    */
 /* ======================================================================== */

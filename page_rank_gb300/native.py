@@ -41,6 +41,7 @@ GL_I32, GL_I64 = 0, 1
 GL_F32, GL_F64 = 0, 1
 GL_PPR_STOP_ALL, GL_PPR_STOP_PER_COLUMN = 0, 1
 GL_DANGLING_TO_TELEPORT, GL_DANGLING_UNIFORM = 0, 1
+GL_SPMM_STATIC_SCRATCH_BYTES = 16 * 1024 * 1024
 GL_MLP_MAX_IN, GL_MLP_HIDDEN = 16, 128
 
 
@@ -159,6 +160,7 @@ _SIGS = {
     "gl_pbr_schedule_build": (_c.c_int, [_c.POINTER(PbrMatrixDesc), _i32, _vp, _i64, _vp]),
     "gl_pbr_spmm_workspace_bytes": (_i64, [_c.POINTER(PbrMatrixDesc), _i64, _i64]),
     "gl_pbr_spmm": (_c.c_int, [_c.POINTER(PbrMatrixDesc), _vp, _vp, _i64, _i64, _vp, _i64, _vp]),
+    "gl_pbr_spmm_static": (_c.c_int, [_c.POINTER(PbrMatrixDesc), _vp, _vp, _i64, _i64, _vp]),
     "gl_ppr_teleport_index": (_c.c_int, [_i64, _i32, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp,
                                          _vp]),
     "gl_ppr_init": (_c.c_int, [_c.POINTER(TeleportDesc), _i64, _i64, _i32, _vp, _vp, _vp, _vp]),
