@@ -60,6 +60,9 @@ int gl_version(void);
  * fills it: stripes holding more than 2 * piece_work stored entries are cut
  * into pieces of piece_work entries, processed independently and reduced in
  * piece order.  column_tile caps the columns one warp covers (0: automatic).
+ * lane_split picks how a warp's lanes share a stripe for 64..127 columns:
+ * 0 automatic, 1 all 32 lanes on each nonzero, 2 two half-warps taking
+ * alternate nonzeros (float4 lanes).
  */
 typedef struct gl_pbr_matrix {
     int64_t rows, cols;
@@ -75,7 +78,7 @@ typedef struct gl_pbr_matrix {
     const void*    remainder_data;      /* [remainder_nnz]                   */
     const int32_t* stripe_block_ptr;    /* [ceil(rows/block_rows) + 1]       */
     /* load-balance schedule (see above) */
-    int32_t num_heavy, num_pieces, piece_work, column_tile;
+    int32_t num_heavy, num_pieces, piece_work, column_tile, lane_split;
     const int32_t* heavy_of;            /* [num_stripes]: heavy index or -1  */
     const int32_t* heavy_stripe;        /* [num_heavy]                       */
     const int32_t* heavy_first;         /* [num_heavy + 1]: first piece      */

@@ -265,7 +265,7 @@ extern "C" int gl_pbr_spmm(const gl_pbr_matrix* A, const void* X, void* Y, int64
         a.X = static_cast<const float*>(X);
         a.Y = static_cast<float*>(Y);
         if ((rc = bind_workspace(a, A, batch, features, workspace, workspace_bytes)) != GL_OK) return rc;
-        return launch_stripe<float, false>(a, A->block_rows, A->block_cols, A->column_tile, stream);
+        return launch_stripe<float, false>(a, A->block_rows, A->block_cols, A->column_tile, A->lane_split, stream);
     }
     StripeArgs<double> a = make_args<double>(A);
     a.batch = batch;
@@ -273,7 +273,7 @@ extern "C" int gl_pbr_spmm(const gl_pbr_matrix* A, const void* X, void* Y, int64
     a.X = static_cast<const double*>(X);
     a.Y = static_cast<double*>(Y);
     if ((rc = bind_workspace(a, A, batch, features, workspace, workspace_bytes)) != GL_OK) return rc;
-    return launch_stripe<double, false>(a, A->block_rows, A->block_cols, A->column_tile, stream);
+    return launch_stripe<double, false>(a, A->block_rows, A->block_cols, A->column_tile, A->lane_split, stream);
 }
 
 extern "C" int gl_pbr_stripe_index(const int32_t* block_coords, int64_t num_blocks, int64_t rows, int32_t block_rows,
@@ -409,14 +409,14 @@ extern "C" int gl_ppr_step(const gl_pbr_matrix* A, const gl_teleport* tp, const 
         a.X = static_cast<const float*>(X_in);
         a.Y = static_cast<float*>(X_out);
         if ((rc = bind_workspace(a, A, 1, K, workspace, workspace_bytes)) != GL_OK) return rc;
-        return launch_stripe<float, true>(a, A->block_rows, A->block_cols, A->column_tile, stream);
+        return launch_stripe<float, true>(a, A->block_rows, A->block_cols, A->column_tile, A->lane_split, stream);
     }
     StripeArgs<double> a = make_args<double>(A);
     GL_FILL_PPR(a);
     a.X = static_cast<const double*>(X_in);
     a.Y = static_cast<double*>(X_out);
     if ((rc = bind_workspace(a, A, 1, K, workspace, workspace_bytes)) != GL_OK) return rc;
-    return launch_stripe<double, true>(a, A->block_rows, A->block_cols, A->column_tile, stream);
+    return launch_stripe<double, true>(a, A->block_rows, A->block_cols, A->column_tile, A->lane_split, stream);
 #undef GL_FILL_PPR
 }
 

@@ -127,12 +127,12 @@ extern "C" int gl_pbr_spmm_static(const gl_pbr_matrix* A, const void* X, void* Y
             a.partial = static_cast<float*>(scratch);
             a.counters = reinterpret_cast<int32_t*>(static_cast<char*>(scratch) + partial);
         }
-        return launch_stripe<float, false>(a, A->block_rows, A->block_cols, A->column_tile, stream);
+        return launch_stripe<float, false>(a, A->block_rows, A->block_cols, A->column_tile, A->lane_split, stream);
     }
     StripeArgs<double> a = static_args<double>(A, X, Y, batch, features);
     if (scratch) {
         a.partial = static_cast<double*>(scratch);
         a.counters = reinterpret_cast<int32_t*>(static_cast<char*>(scratch) + partial);
     }
-    return launch_stripe<double, false>(a, A->block_rows, A->block_cols, A->column_tile, stream);
+    return launch_stripe<double, false>(a, A->block_rows, A->block_cols, A->column_tile, A->lane_split, stream);
 }

@@ -5,8 +5,13 @@ namespace gl {
 
 namespace {
 template <bool PPR, int BR>
-int dispatch_f32(const StripeArgs<float>& a, int tile_hint, cudaStream_t st) {
-    const Shape sh = pick_shape<float>(a.K, tile_hint, a.X, a.Y);
+int dispatch_f32(const StripeArgs<float>& a, int tile_hint, int lane_split, cudaStream_t st) {
+    // the half-warp shape is register-heavy with the power-iteration
+    // epilogue, so only the plain SpMM uses it
+    const Shape sh = pick_shape<float>(a.K, tile_hint, a.X, a.Y, !PPR, lane_split);
+    if constexpr (!PPR) {
+        if (sh.V == 4 && sh.C == 16) return launch_stripe_shape<float, BR, 4, 16, PPR>(a, st);
+    }
     switch (sh.V * 100 + sh.C) {
         case 432: return launch_stripe_shape<float, BR, 4, 32, PPR>(a, st);
         case 232: return launch_stripe_shape<float, BR, 2, 32, PPR>(a, st);
@@ -21,21 +26,23 @@ int dispatch_f32(const StripeArgs<float>& a, int tile_hint, cudaStream_t st) {
 }  // namespace
 
 template <bool PPR>
-static int launch_f32(const StripeArgs<float>& a, int br, int bc, int tile_hint, cudaStream_t st) {
-    if (br == 2 && bc == 2) return dispatch_f32<PPR, 2>(a, tile_hint, st);
-    if (br == 4 && bc == 4) return dispatch_f32<PPR, 4>(a, tile_hint, st);
-    if (br == 8 && bc == 8) return dispatch_f32<PPR, 8>(a, tile_hint, st);
+static int launch_f32(const StripeArgs<float>& a, int br, int bc, int tile_hint, int lane_split, cudaStream_t st) {
+    if (br == 2 && bc == 2) return dispatch_f32<PPR, 2>(a, tile_hint, lane_split, st);
+    if (br == 4 && bc == 4) return dispatch_f32<PPR, 4>(a, tile_hint, lane_split, st);
+    if (br == 8 && bc == 8) return dispatch_f32<PPR, 8>(a, tile_hint, lane_split, st);
     set_error("Unsupported block size for PBR SpMM. Only 2x2, 4x4, and 8x8 are supported.");
     return GL_ERR_UNSUPPORTED_BLOCK;
 }
 
 template <>
-int launch_stripe<float, false>(const StripeArgs<float>& a, int br, int bc, int tile_hint, cudaStream_t st) {
-    return launch_f32<false>(a, br, bc, tile_hint, st);
+int launch_stripe<float, false>(const StripeArgs<float>& a, int br, int bc, int tile_hint, int lane_split,
+                            cudaStream_t st) {
+    return launch_f32<false>(a, br, bc, tile_hint, lane_split, st);
 }
 template <>
-int launch_stripe<float, true>(const StripeArgs<float>& a, int br, int bc, int tile_hint, cudaStream_t st) {
-    return launch_f32<true>(a, br, bc, tile_hint, st);
+int launch_stripe<float, true>(const StripeArgs<float>& a, int br, int bc, int tile_hint, int lane_split,
+                            cudaStream_t st) {
+    return launch_f32<true>(a, br, bc, tile_hint, lane_split, st);
 }
 
 }  // namespace gl

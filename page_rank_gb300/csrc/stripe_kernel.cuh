@@ -124,7 +124,7 @@ __device__ __forceinline__ int32_t lower_bound_i32(const int32_t* offsets, int32
 // Decoding is lane-parallel (a few instructions per nonzero spread over the
 // warp); consuming costs one load, one address and V FMAs per nonzero.
 // ---------------------------------------------------------------------------
-constexpr int kListCap = 512;     // entries per warp list (>= 32 blocks x 8 bits)
+constexpr int kListCap = 640;     // entries per warp list: a 512-entry unit plus row padding
 // row gathers in flight per warp: enough bytes in flight per SM at moderate
 // register cost (V = 4 moves 512 B per gather)
 template <int V>
@@ -132,32 +132,34 @@ struct Gather {
     static constexpr int n = V >= 4 ? 4 : 8;
 };
 
-// The list is padded to a multiple of the gather depth with (column 0,
-// value 0) entries, so the loop carries no predicates; lanes past the last
-// column gather from a clamped (valid) address and never store.
-template <typename S, int V>
+// The list is padded to a multiple of (gather depth x nonzero lanes) with
+// (column 0, value 0) entries, so the loop carries no predicates; lanes past
+// the last column gather from a clamped (valid) address and never store.
+// With P = 2 the two half-warps take alternate entries (each half-warp
+// covers the whole column tile with V-wide loads).
+template <typename S, int V, int P>
 __device__ __forceinline__ void consume_list(S (&t)[V], const int32_t* lcol, const S* lval, int n_padded,
-                                             const S* __restrict__ Xb, int32_t K) {
+                                             const S* __restrict__ Xb, int32_t K, int p_lane) {
     constexpr int NG = Gather<V>::n;
-    for (int e0 = 0; e0 < n_padded; e0 += NG) {
+    for (int e0 = p_lane; e0 < n_padded; e0 += NG * P) {
         Pack<S, V> x[NG];
 #pragma unroll
-        for (int q = 0; q < NG; ++q) x[q] = load_pack<S, V>(Xb + (long long)lcol[e0 + q] * K);
+        for (int q = 0; q < NG; ++q) x[q] = load_pack<S, V>(Xb + (long long)lcol[e0 + q * P] * K);
 #pragma unroll
         for (int q = 0; q < NG; ++q) {
-            const S v = lval[e0 + q];
+            const S v = lval[e0 + q * P];
 #pragma unroll
             for (int j = 0; j < V; ++j) t[j] = fma(v, x[q].v[j], t[j]);
         }
     }
 }
 
-// Pads the list [0, n) with (0, 0) entries up to a multiple of the gather
-// depth (never past kListCap, which is a multiple of it); returns the padded length.
-template <typename S, int V>
+// Pads the list [0, n) with (0, 0) entries up to a multiple of NG * P (never
+// past kListCap, which is a multiple of it); returns the padded length.
+template <typename S, int V, int P>
 __device__ __forceinline__ int pad_list(int32_t* lcol, S* lval, int n, int lane) {
-    constexpr int NG = Gather<V>::n;
-    const int np = (n + NG - 1) / NG * NG;
+    constexpr int NGP = Gather<V>::n * P;
+    const int np = (n + NGP - 1) / NGP * NGP;
     if (lane < np - n) {
         lcol[n + lane] = 0;
         lval[n + lane] = S(0);
@@ -166,14 +168,52 @@ __device__ __forceinline__ int pad_list(int32_t* lcol, S* lval, int n, int lane)
     return np;
 }
 
-template <typename S, int BR, int BC, int V>
+// Packed per-row counters: row r's count sits in 16-bit field r % 4 of word
+// r / 4, so one 64-bit warp scan per word yields every row's offsets.
+template <int BR>
+struct RowPack {
+    static constexpr int W = (BR + 3) / 4;
+    uint64_t w[W];
+    __device__ __forceinline__ void clear() {
+#pragma unroll
+        for (int i = 0; i < W; ++i) w[i] = 0;
+    }
+    __device__ __forceinline__ void set(int r, uint32_t v) { w[r >> 2] |= (uint64_t)v << (16 * (r & 3)); }
+    __device__ __forceinline__ uint32_t get(int r) const { return (uint32_t)(w[r >> 2] >> (16 * (r & 3))) & 0xffffu; }
+};
+
+template <typename S, int BR, int BC, int V, int P>
 __device__ __forceinline__ void accumulate_lists(const StripeArgs<S>& a, S (&acc)[BR][V], unsigned char* smem_raw,
                                                  int64_t s, int32_t b0, int32_t b1, int32_t j0, int32_t j1,
-                                                 const S* __restrict__ Xb, bool lane_ok, int lane) {
+                                                 const S* __restrict__ Xb, bool lane_ok, int lane, int p_lane) {
     constexpr uint32_t ROWMASK = (BC >= 32) ? 0xffffffffu : ((1u << BC) - 1u);
+    constexpr int NG = Gather<V>::n * P;   // list granule: every nonzero lane gets full gather batches
     const int warp = threadIdx.x >> 5;
     int32_t* lcol = reinterpret_cast<int32_t*>(smem_raw) + warp * kListCap;
     S* lval = reinterpret_cast<S*>(smem_raw + (size_t)kStripeWarps * kListCap * sizeof(int32_t)) + warp * kListCap;
+    // per-row bookkeeping of this warp: [rstart | rlen | seg | blen] x BR
+    int32_t* rowinfo = reinterpret_cast<int32_t*>(smem_raw + (size_t)kStripeWarps * kListCap *
+                                                                 (sizeof(int32_t) + sizeof(S))) + warp * 4 * BR;
+    int32_t* rstart = rowinfo;
+    int32_t* rlen = rowinfo + BR;
+    int32_t* seg = rowinfo + 2 * BR;
+    int32_t* blen = rowinfo + 3 * BR;
+
+    // remainder row ranges of this unit (lane r computes row r)
+    if (lane < BR) {
+        const int64_t row = s * BR + lane;
+        int32_t rs = j1, re = j1;
+        if (row < a.rows) {
+            rs = a.rem_ptr[row];
+            re = a.rem_ptr[row + 1];
+            rs = rs > j0 ? rs : j0;
+            re = re < j1 ? re : j1;
+            re = re > rs ? re : rs;
+        }
+        rstart[lane] = rs;
+        rlen[lane] = re - rs;
+    }
+    __syncwarp();
 
     for (int32_t kc = b0; kc < b1 || kc == b0; kc += 32) {
         const int32_t nb = (b1 - kc) < 32 ? (b1 - kc > 0 ? b1 - kc : 0) : 32;
@@ -185,66 +225,134 @@ __device__ __forceinline__ void accumulate_lists(const StripeArgs<S>& a, S (&acc
             col0 = a.coords[2 * (int64_t)(kc + lane) + 1];
             off = a.offsets[kc + lane];
         }
+        // per-row bit counts of this lane's block, scanned over the warp
+        RowPack<BR> cnt, incl;
+        cnt.clear();
+#pragma unroll
+        for (int r = 0; r < BR; ++r) cnt.set(r, __popc((uint32_t)(code >> (r * BC)) & ROWMASK));
+        uint64_t tot_lane = 0;   // lane r / 4 holds the totals word r / 4 after this
+#pragma unroll
+        for (int i = 0; i < RowPack<BR>::W; ++i) {
+            uint64_t v = cnt.w[i];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint64_t u = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o) v += u;
+            }
+            incl.w[i] = v;
+            const uint64_t t = __shfl_sync(0xffffffffu, v, 31);
+            if ((lane >> 2) == i) tot_lane = t;
+        }
+        // row segments [block entries | remainder entries | padding]:
+        // lane r < BR owns row r; a scan over those lanes places them
+        int32_t my_len = 0, my_blen = 0;
+        if (lane < BR) {
+            my_blen = (int32_t)((tot_lane >> (16 * (lane & 3))) & 0xffffu);
+            my_len = my_blen + (last ? rlen[lane] : 0);
+        }
+        const int32_t padded = (my_len + NG - 1) / NG * NG;
+        const int32_t incl_pad = (int32_t)warp_incl_scan_i64(padded);
+        const int32_t total = __shfl_sync(0xffffffffu, incl_pad, BR - 1);
+        if (lane < BR) {
+            seg[lane] = incl_pad - padded;
+            blen[lane] = my_blen;
+        }
+        __syncwarp();
+        if (total <= kListCap) {
+            // this lane's block entries into its rows' segments
+            if (code) {
+                int32_t k = off;
+#pragma unroll
+                for (int r = 0; r < BR; ++r) {
+                    uint32_t rb = (uint32_t)(code >> (r * BC)) & ROWMASK;
+                    int pos = seg[r] + (int)(incl.get(r) - cnt.get(r));
+                    while (rb) {
+                        const int c = __ffs(rb) - 1;
+                        rb &= rb - 1u;
+                        lcol[pos] = col0 + c;
+                        lval[pos] = a.bdata[k++];
+                        ++pos;
+                    }
+                }
+            }
+            // remainder entries (last chunk) and padding, lane-parallel
 #pragma unroll 1
-        for (int r = 0; r < BR; ++r) {
-            // accumulators of row r, moved to a statically indexed temporary
-            S t[V];
-#pragma unroll
-            for (int j = 0; j < V; ++j) t[j] = S(0);
-#pragma unroll
-            for (int rr = 0; rr < BR; ++rr)
-                if (rr == r) {
-#pragma unroll
-                    for (int j = 0; j < V; ++j) t[j] = acc[rr][j];
+            for (int r = 0; r < BR; ++r) {
+                const int32_t sg = seg[r], bl = blen[r];
+                const int32_t rl = last ? rlen[r] : 0;
+                const int32_t rs = rstart[r];
+                for (int q = lane; q < rl; q += 32) {
+                    lcol[sg + bl + q] = a.rem_col[rs + q];
+                    lval[sg + bl + q] = a.rem_val[rs + q];
                 }
-            // ---- decode the chunk's bits of row r into the list -------------
-            uint32_t rb = (uint32_t)(code >> (r * BC)) & ROWMASK;
-            const int cnt = __popc(rb);
-            int pos = (int)warp_incl_scan_i64(cnt) - cnt;
-            const int nblk = __shfl_sync(0xffffffffu, pos + cnt, 31);
-            if (rb) {
-                int32_t k = off + (r == 0 ? 0 : __popcll(code & ((1ull << (r * BC)) - 1ull)));
-                while (rb) {
-                    const int c = __ffs(rb) - 1;
-                    rb &= rb - 1u;
-                    lcol[pos] = col0 + c;
-                    lval[pos] = a.bdata[k++];
-                    ++pos;
+                const int32_t len = bl + rl;
+                const int32_t pad = (len + NG - 1) / NG * NG - len;
+                if (lane < pad) {
+                    lcol[sg + len + lane] = 0;
+                    lval[sg + len + lane] = S(0);
                 }
             }
-            int n = nblk;
-            // ---- append the row's remainder entries (last chunk only) ----------
-            const int64_t row = s * BR + r;
-            if (last && row < a.rows) {
-                int32_t rs = a.rem_ptr[row], re = a.rem_ptr[row + 1];
-                rs = rs > j0 ? rs : j0;
-                re = re < j1 ? re : j1;
-                while (rs < re) {
-                    const int room = kListCap - Gather<V>::n - n;
-                    const int take = (re - rs) < room ? (re - rs) : room;
-                    for (int q = lane; q < take; q += 32) {
-                        lcol[n + q] = a.rem_col[rs + q];
-                        lval[n + q] = a.rem_val[rs + q];
+            __syncwarp();
+#pragma unroll
+            for (int r = 0; r < BR; ++r) {
+                const int32_t len = blen[r] + (last ? rlen[r] : 0);
+                consume_list<S, V, P>(acc[r], lcol + seg[r], lval + seg[r], (len + NG - 1) / NG * NG, Xb, a.K,
+                                      p_lane);
+            }
+            __syncwarp();
+        } else {
+            // too many entries for one list: one row at a time, remainder in
+            // list-sized pieces
+#pragma unroll 1
+            for (int r = 0; r < BR; ++r) {
+                S t[V];
+#pragma unroll
+                for (int j = 0; j < V; ++j) t[j] = S(0);
+                uint32_t rb = (uint32_t)(code >> (r * BC)) & ROWMASK;
+                if (rb) {
+                    int pos = (int)(incl.get(r) - cnt.get(r));
+                    int32_t k = off + (r == 0 ? 0 : __popcll(code & ((1ull << (r * BC)) - 1ull)));
+                    while (rb) {
+                        const int c = __ffs(rb) - 1;
+                        rb &= rb - 1u;
+                        lcol[pos] = col0 + c;
+                        lval[pos] = a.bdata[k++];
+                        ++pos;
                     }
-                    __syncwarp();
-                    n += take;
-                    rs += take;
-                    if (rs < re) {   // list full: consume and continue
-                        consume_list<S, V>(t, lcol, lval, pad_list<S, V>(lcol, lval, n, lane), Xb, a.K);
+                }
+                int n = blen[r];
+                if (last) {
+                    int32_t rs = rstart[r];
+                    const int32_t re = rstart[r] + rlen[r];
+                    while (rs < re) {
+                        const int room = kListCap - NG - n;
+                        const int take = (re - rs) < room ? (re - rs) : room;
                         __syncwarp();
-                        n = 0;
+                        for (int q = lane; q < take; q += 32) {
+                            lcol[n + q] = a.rem_col[rs + q];
+                            lval[n + q] = a.rem_val[rs + q];
+                        }
+                        __syncwarp();
+                        n += take;
+                        rs += take;
+                        if (rs < re) {
+                            consume_list<S, V, P>(t, lcol, lval, pad_list<S, V, P>(lcol, lval, n, lane), Xb,
+                                                  a.K, p_lane);
+                            __syncwarp();
+                            n = 0;
+                        }
                     }
                 }
+                __syncwarp();
+                consume_list<S, V, P>(t, lcol, lval, pad_list<S, V, P>(lcol, lval, n, lane), Xb, a.K, p_lane);
+                __syncwarp();
+#pragma unroll
+                for (int rr = 0; rr < BR; ++rr)
+                    if (rr == r) {
+#pragma unroll
+                        for (int j = 0; j < V; ++j) acc[rr][j] += t[j];
+                    }
             }
-            __syncwarp();
-            consume_list<S, V>(t, lcol, lval, pad_list<S, V>(lcol, lval, n, lane), Xb, a.K);
-            __syncwarp();
-#pragma unroll
-            for (int rr = 0; rr < BR; ++rr)
-                if (rr == r) {
-#pragma unroll
-                    for (int j = 0; j < V; ++j) acc[rr][j] = t[j];
-                }
         }
         if (kc >= b1) break;   // empty block range: one pass for the remainder
     }
@@ -253,18 +361,20 @@ __device__ __forceinline__ void accumulate_lists(const StripeArgs<S>& a, S (&acc
 // Dynamic shared memory of one CTA of stripe_kernel.
 template <typename S, int BC, int V, int C>
 constexpr size_t stripe_smem_bytes() {
-    return (32 / C == 1) ? (size_t)kStripeWarps * kListCap * (sizeof(int32_t) + sizeof(S))
+    return (32 / C <= 2) ? (size_t)kStripeWarps * kListCap * (sizeof(int32_t) + sizeof(S)) +
+                               (size_t)kStripeWarps * 4 * BC * sizeof(int32_t)
                          : (size_t)BC * kStripeThreads * V * sizeof(S);
 }
 
 // Minimum resident CTAs per SM the register allocation must allow.
-template <int V>
+// (the power-iteration epilogue needs more registers than the plain store)
+template <int V, bool PPR, int C>
 struct MinBlocks {
-    static constexpr int n = V >= 4 ? 2 : 3;
+    static constexpr int n = (V >= 4 && C == 32) ? 2 : (PPR || V >= 4 ? 3 : 4);
 };
 
 template <typename S, int BR, int BC, int V, int C, bool PPR>
-__global__ void __launch_bounds__(kStripeThreads, MinBlocks<V>::n)
+__global__ void __launch_bounds__(kStripeThreads, MinBlocks<V, PPR, C>::n)
 stripe_kernel(const StripeArgs<S> a) {
     constexpr int P = 32 / C;            // nonzero lanes per warp
     constexpr int T = C * V;             // columns per tile
@@ -411,8 +521,8 @@ stripe_kernel(const StripeArgs<S> a) {
         // lanes past the last column read a valid address and never store
         const S* __restrict__ Xb = a.X + b * a.cols * (int64_t)a.K + (lane_ok ? col_base : 0);
 
-        if constexpr (P == 1) {
-            accumulate_lists<S, BR, BC, V>(a, acc, xs_dyn, s, b0, b1, j0, j1, Xb, lane_ok, lane);
+        if constexpr (P <= 2) {
+            accumulate_lists<S, BR, BC, V, P>(a, acc, xs_dyn, s, b0, b1, j0, j1, Xb, lane_ok, lane, p_lane);
         } else {
             // ---- PBR blocks: lanes stride the blocks ------------------------
             for (int32_t kb = b0 + p_lane; kb < b1; kb += P) {
@@ -595,7 +705,8 @@ stripe_kernel(const StripeArgs<S> a) {
 // Host-side launcher for one (S, PPR) family; picks the block shape, the
 // vector width V and the column-lane count C.  Returns a GL_* status.
 template <typename S, bool PPR>
-int launch_stripe(const StripeArgs<S>& a0, int block_rows, int block_cols, int tile_hint, cudaStream_t stream);
+int launch_stripe(const StripeArgs<S>& a0, int block_rows, int block_cols, int tile_hint, int lane_split,
+                  cudaStream_t stream);
 
 // Columns per tile the launcher will use for K columns (for workspace sizing).
 template <typename S>

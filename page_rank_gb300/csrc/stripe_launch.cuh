@@ -40,13 +40,18 @@ struct Shape {
 };
 
 template <typename S>
-Shape pick_shape(int64_t K, int tile_hint, const void* X, const void* Y) {
+Shape pick_shape(int64_t K, int tile_hint, const void* X, const void* Y, bool allow_half_warps = true,
+                 int lane_split = 0) {
     auto vec_ok = [&](int v) {
         return K % v == 0 && aligned_to(X, v * (int)sizeof(S)) && aligned_to(Y, v * (int)sizeof(S));
     };
     const int max_v = sizeof(S) == 4 ? 4 : 2;
     int cap = tile_hint > 0 ? tile_hint : 1 << 30;
     if (sizeof(S) == 8 && K < 17) return {1, 1};   // FP64 instantiates only C = 1 below 17 columns
+    // 64 <= K < 128 (FP32): two half-warps with float4 lanes each cover 64
+    // columns and take alternate nonzeros
+    if (allow_half_warps && lane_split == 2 && sizeof(S) == 4 && K >= 64 && K < 128 && 64 <= cap && vec_ok(4))
+        return {4, 16};
     if (K >= 32) {
         for (int v = max_v; v >= 1; v >>= 1)
             if (K >= 32 * v && 32 * v <= cap && vec_ok(v)) return {v, 32};

@@ -56,9 +56,8 @@ class PPREngine:
 
     def __init__(self, A: sp.csr_matrix, block_size: int = 8, min_nnz_per_block: int | None = None,
                  device=None, dangling: np.ndarray | None = None, column_tile: int = 0):
-        if device is None:
-            device = torch.device("cuda", torch.cuda.current_device())
-        self.device = torch.device(device)
+        dev = torch.device(device) if device is not None else torch.device("cuda")
+        self.device = dev if dev.index is not None else torch.device("cuda", torch.cuda.current_device())
         if A.shape[0] != A.shape[1]:
             raise ValueError("transition matrix must be square")
         if not A.has_canonical_format:
@@ -82,12 +81,19 @@ class PPREngine:
             else:
                 self.dbits = _bitmap_from_mask(np.asarray(dangling, bool), self.device)
         self.nnz = int(A.nnz)
+        self.host_indptr = A.indptr
+        self.host_indices = A.indices
         self._graphs: dict = {}
 
     # -- sizes ----------------------------------------------------------------
     def matrix_bytes(self) -> int:
-        m = self.meta
-        return int(sum(t.numel() * t.element_size() for k, t in m.items()))
+        """Device bytes of the resident matrix (PBR arrays, stripe index,
+        load-balance schedule)."""
+        tot = sum(t.numel() * t.element_size() for t in self.meta.values() if isinstance(t, torch.Tensor))
+        sched = self.meta.get("schedule")
+        if sched is not None:
+            tot += sched["buffer"].numel() * sched["buffer"].element_size()
+        return int(tot + self.dbits.numel() * self.dbits.element_size())
 
     def iteration_bytes(self, k: int) -> int:
         """Algorithmic HBM bytes of one fused step with k columns: the matrix
@@ -121,6 +127,15 @@ class PPREngine:
         dev = self.device
         return (torch.from_numpy(ptr2).to(dev), torch.from_numpy(rows).to(dev),
                 torch.from_numpy(w).to(dev))
+
+    def teleport_columns(self, seed_sets) -> torch.Tensor:
+        """Dense teleport (personalization) vectors [n, K] of the seed sets."""
+        ptr, rows, w = self.teleport(seed_sets)
+        tp = teleport_from_seed_sets(ptr, rows, self.n, self.block_size, w)
+        V = torch.empty((self.n, len(seed_sets)), dtype=torch.float32, device=self.device)
+        native.check(native.lib().gl_ppr_init(tp.desc(), self.n, len(seed_sets), native.GL_F32, V.data_ptr(),
+                                              None, None, torch.cuda.current_stream(self.device).cuda_stream))
+        return V
 
     def solve(self, seed_sets, alpha: float = 0.85, tol: float = 1e-6, max_iterations: int = 1000,
               certified: bool = True, retire: bool = True, chunk: int = 8, x0: torch.Tensor | None = None,

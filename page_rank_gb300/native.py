@@ -125,6 +125,7 @@ class PbrMatrixDesc(_c.Structure):
                 ("block_data", _vp), ("remainder_indptr", _vp), ("remainder_col_ind", _vp),
                 ("remainder_data", _vp), ("stripe_block_ptr", _vp),
                 ("num_heavy", _i32), ("num_pieces", _i32), ("piece_work", _i32), ("column_tile", _i32),
+                ("lane_split", _i32),
                 ("heavy_of", _vp), ("heavy_stripe", _vp), ("heavy_first", _vp), ("piece_heavy", _vp)]
 
 

@@ -293,6 +293,7 @@ def matrix_desc(meta: dict, rows: int, cols: int, block_rows: int, block_cols: i
     d.remainder_data = _ptr(meta["rem_vals"])
     d.stripe_block_ptr = _ptr(meta["stripe_ptr"])
     d.column_tile = int(meta.get("column_tile", 0))
+    d.lane_split = int(meta.get("lane_split", 0))
     sched = meta.get("schedule")
     if sched is None and block_rows == block_cols and block_rows in (2, 4, 8) and rows > 0:
         sched = build_schedule(d, meta["stripe_ptr"].device, int(meta.get("piece_work", 0)))

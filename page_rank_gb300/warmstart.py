@@ -118,14 +118,12 @@ class WarmStart:
         self.dev = engine.device
         self.mlp = MLP(self.dev, seed)
         n = engine.n
-        indptr = engine.pbr._build.rem_indptr  # placeholder to keep device; degrees below
         A_rows = torch.as_tensor(np.diff(engine.host_indptr), device=self.dev, dtype=torch.float32)
         out_deg = torch.bincount(torch.as_tensor(engine.host_indices, device=self.dev, dtype=torch.int64),
                                  minlength=n).to(torch.float32)
         self.log_in = torch.log1p(A_rows)
         self.log_out = torch.log1p(out_deg)
         self._desc = matrix_desc(engine.meta, n, n, engine.block_size, engine.block_size)
-        del indptr
 
     # -- features -------------------------------------------------------------
     def _spmm(self, X: torch.Tensor) -> torch.Tensor:
@@ -139,13 +137,7 @@ class WarmStart:
         return Y
 
     def seed_matrix(self, seed_sets) -> torch.Tensor:
-        ptr, rows, w = self.eng.teleport(seed_sets)
-        tp = teleport_from_seed_sets(ptr, rows, self.eng.n, self.eng.block_size, w)
-        V = torch.empty((self.eng.n, len(seed_sets)), dtype=torch.float32, device=self.dev)
-        native.check(native.lib().gl_ppr_init(tp.desc(), self.eng.n, len(seed_sets), native.GL_F32,
-                                              V.data_ptr(), None, None,
-                                              torch.cuda.current_stream(self.dev).cuda_stream))
-        return V
+        return self.eng.teleport_columns(seed_sets)
 
     def raw_features(self, V: torch.Tensor):
         """(m1, m2, hop) for the columns of V; hop in 0..5 (5 = farther than 4)."""
@@ -181,8 +173,8 @@ class WarmStart:
 
     # -- training ---------------------------------------------------------------
     def train(self, num_vectors: int = 20000, batch: int = 256, nodes_per_vector: int = 512,
-              alpha: float = 0.85, tol: float = 1e-6, lr: float = 2e-3, minibatch: int = 65536,
-              epochs: int = 2, seed: int = 100) -> TrainStats:
+              alpha: float = 0.85, tol: float = 1e-6, lr: float = 3e-3, minibatch: int = 8192,
+              epochs: int = 6, seed: int = 100) -> TrainStats:
         """Solve num_vectors seed sets (sizes 1-32) with the plain method (the
         engine without warm start) and fit the network to their log-PPR on
         sampled nodes (most by PPR mass, some uniform)."""
@@ -214,13 +206,18 @@ class WarmStart:
         T = torch.cat(targs)
         n = Xf.shape[0]
         losses = []
+        steps_total = epochs * ((n + minibatch - 1) // minibatch)
+        step = 0
         for _ in range(epochs):
             perm = torch.randperm(n, device=self.dev, generator=gen)
             for s0 in range(0, n, minibatch):
                 sel = perm[s0:s0 + minibatch]
                 _, loss = self.mlp.gradient(Xf[sel], T[sel])
-                self.mlp.adam_step(sel.numel(), lr)
+                # cosine decay from lr to lr / 10
+                cur = lr * (0.1 + 0.9 * 0.5 * (1.0 + math.cos(math.pi * step / max(1, steps_total))))
+                self.mlp.adam_step(sel.numel(), cur)
                 losses.append(loss / sel.numel())
+                step += 1
         torch.cuda.synchronize(self.dev)
         return TrainStats(vectors=num_vectors, examples=n, seconds=time.perf_counter() - t0, losses=losses)
 

@@ -77,3 +77,97 @@ def ppr_batched(device, log2n: int = 22, K: int = 256, plain_sample: int = 16, t
         "max_l1_batched_vs_plain": diff,
         "iteration_bytes_full_width": step_bytes,
     }
+
+
+def warmstart(device, log2n: int = 21, train_vectors: int = 20000, K: int = 256) -> dict:
+    """Learned warm start on the cluster / Zipf graph class at n = 2**log2n:
+    train on ``train_vectors`` plain-method PPR vectors (seed sets of 1-32),
+    then solve K held-out seed sets from the predicted start and from the
+    cold start, both to the certified L1 1e-6."""
+    from .warmstart import WarmStart
+    g = synth.cluster_zipf_graph(log2n=log2n, mean_degree=20.0, seed=3, device=device)
+    eng = PPREngine(g.A, block_size=8, min_nnz_per_block=4, device=device, dangling=g.dangling)
+    ws = WarmStart(eng, seed=0)
+    stats = ws.train(num_vectors=train_vectors, batch=256, nodes_per_vector=512, epochs=3)
+    sets = synth.seed_sets(g.n, K, 1, 32, seed=424242)
+    eng.solve(sets[:8], tol=1e-6)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    cold = eng.solve(sets, tol=1e-6)
+    t_cold = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    warm = ws.solve(sets, tol=1e-6)
+    t_warm = time.perf_counter() - t0
+    diff = (cold.X.double() - warm.X.double()).abs().sum(dim=0).max().item()
+    return {
+        "workload": f"warmstart: {g.description}, MLP 10-128-1 BF16 weights, trained on {train_vectors} "
+                    f"plain-method vectors, {K} held-out seed sets of 1-32",
+        "n": g.n, "nnz": int(g.A.nnz),
+        "train": {"vectors": stats.vectors, "examples": stats.examples, "seconds": round(stats.seconds, 2),
+                  "loss_first": stats.losses[0], "loss_last": stats.losses[-1]},
+        "cold": {"iterations_sum": int(cold.iterations.sum()), "iterations_max": int(cold.iterations.max()),
+                 "seconds": round(t_cold, 4), "column_steps": cold.column_steps},
+        "warm": {"iterations_sum": int(warm.iterations.sum()), "iterations_max": int(warm.iterations.max()),
+                 "seconds_including_prediction": round(t_warm, 4), "column_steps": warm.column_steps,
+                 "columns_using_prediction": float(warm.warm_columns.mean())},
+        "iteration_ratio_cold_over_warm": round(float(cold.iterations.sum() / max(1, warm.iterations.sum())), 3),
+        "max_l1_cold_vs_warm": diff,
+    }
+
+
+def serving(device, rates=(200.0, 800.0, 3200.0), requests_per_rate: int = 400, graphs: int = 8,
+            warm: bool = True, seed: int = 5) -> dict:
+    """8 resident cluster / Zipf graphs with n log-uniform in 2**16 .. 2**22,
+    Poisson arrivals at each rate, 1-64 seeds per request, alpha in
+    {0.8, 0.85, 0.9}, certified L1 1e-6; p50 / p99 latency and queries/s."""
+    from .serving import PPRServer, latency_summary
+    from .warmstart import WarmStart
+    rng = np.random.default_rng(seed)
+    sizes = np.sort(np.round(rng.uniform(16, 22, graphs)).astype(int))
+    srv = PPRServer(device=device, chunk=8)
+    descr = []
+    ws_model = None
+    if warm:
+        gt = synth.cluster_zipf_graph(log2n=16, mean_degree=20.0, seed=99)
+        et = PPREngine(gt.A, block_size=8, min_nnz_per_block=4, device=device, dangling=gt.dangling)
+        ws_model = WarmStart(et, seed=0)
+        ws_model.train(num_vectors=4096, batch=256, nodes_per_vector=512, epochs=6)
+    for i, lg in enumerate(sizes):
+        g = synth.cluster_zipf_graph(log2n=int(lg), mean_degree=20.0, seed=200 + i, device=device)
+        eng = srv.add_graph(f"g{i}", g.A, dangling=g.dangling, block_size=8, min_nnz=4)
+        if ws_model is not None:
+            w = WarmStart(eng, seed=0)
+            w.mlp = ws_model.mlp          # one model for the whole graph class
+            srv.warm[f"g{i}"] = w
+        descr.append(int(g.n))
+    # warm up every graph once
+    for i in range(graphs):
+        srv.submit(f"g{i}", [0, 1])
+    srv.run_until_idle()
+    out = {"workload": f"serving: {graphs} cluster/Zipf graphs, n = {descr}, Poisson arrivals, 1-64 seeds, "
+                       f"alpha in {{.8,.85,.9}}, certified L1 1e-6, warm start {'on' if warm else 'off'}",
+           "resident_bytes": srv.resident_bytes(), "rates": []}
+    srv.start()
+    try:
+        for lam in rates:
+            srv.completed.clear()
+            reqs = []
+            t0 = time.perf_counter()
+            for _ in range(requests_per_rate):
+                i = int(rng.integers(0, graphs))
+                n = descr[i]
+                seeds = rng.choice(n, size=int(rng.integers(1, 65)), replace=False)
+                reqs.append(srv.submit(f"g{i}", seeds, alpha=float(rng.choice([0.8, 0.85, 0.9])), tol=1e-6))
+                time.sleep(float(rng.exponential(1.0 / lam)))
+            for r in reqs:
+                r.done.wait(600)
+            wall = time.perf_counter() - t0
+            s = latency_summary(reqs)
+            s.update({"offered_qps": lam, "achieved_qps": round(len(reqs) / wall, 1),
+                      "converged": int(sum(r.converged for r in reqs)),
+                      "mean_iterations": round(float(np.mean([r.iterations for r in reqs])), 1)})
+            out["rates"].append(s)
+    finally:
+        srv.stop()
+    out["admission_waits"] = srv.admission_waits
+    return out

@@ -157,3 +157,17 @@ def test_to_semantics(device):
     assert gl.get_pbr_gpu_meta(c) is None
     gl.clear_pbr_gpu_meta(q)
     assert gl.get_pbr_gpu_meta(q) is None
+
+
+def test_host_batches_pipeline(device):
+    """spmm_host_batches: host batches in, host results out, copies overlapped."""
+    from page_rank_gb300.streaming import spmm_host_batches
+    gl = _gl()
+    A = random_csr(512, 0.05)
+    pbr = gl.csr_to_pbr(A, 8, 8, 4).to(device)
+    xs = [torch.from_numpy(random_x(512, 64, seed=s)).pin_memory() for s in range(5)]
+    ys = [torch.empty(512, 64).pin_memory() for _ in range(5)]
+    spmm_host_batches(pbr, xs, ys)
+    torch.cuda.synchronize()
+    for x, y in zip(xs, ys):
+        _check(y.numpy(), spmm_csr_fp64(A, x.numpy()))

@@ -1,0 +1,82 @@
+"""Host-side logic that needs no GPU: normalize_transition_matrix against the
+reference's own output (golden), the sparse normalization used in-kernel,
+dtype dispatch, error behaviour without a device, synthetic generators."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import torch
+
+from tests._cases import GOLDEN
+
+
+def test_normalize_matches_reference_golden():
+    from page_rank_gb300 import graph_link as gl
+    z = np.load(GOLDEN / "normalize_cases.npz")
+    for i in range(int(z["count"])):
+        k = f"c{i}"
+        A = sp.csr_matrix((z[f"{k}/data"], z[f"{k}/indices"], z[f"{k}/indptr"]), shape=tuple(z[f"{k}/shape"]))
+        out = gl.normalize_transition_matrix(A)
+        assert np.array_equal(out.indptr, z[f"{k}/out_indptr"])
+        assert np.array_equal(out.indices, z[f"{k}/out_indices"])
+        assert np.array_equal(out.data.view(np.uint8), z[f"{k}/out_data"].view(np.uint8))
+
+
+def test_sparse_normalization_agrees_off_dangling_columns():
+    from page_rank_gb300 import graph_link as gl
+    from page_rank_gb300.transition import normalize_columns
+    z = np.load(GOLDEN / "normalize_cases.npz")
+    A = sp.csr_matrix((z["c0/data"], z["c0/indices"], z["c0/indptr"]), shape=tuple(z["c0/shape"]))
+    dense = gl.normalize_transition_matrix(A).toarray()
+    sparse, dmask = normalize_columns(A)
+    s = sparse.toarray()
+    assert np.array_equal(s[:, ~dmask], dense[:, ~dmask])
+    assert (s[:, dmask] == 0).all() and np.allclose(dense[:, dmask], 1.0 / A.shape[0])
+
+
+def test_pybind_overload_order_dtype_dispatch():
+    from page_rank_gb300.graph_link import _dtypes
+    i32, i64 = np.zeros(1, np.int32), np.zeros(1, np.int64)
+    f32, f64 = np.zeros(1, np.float32), np.zeros(1, np.float64)
+    assert _dtypes(i32, i32, f32) == (np.int32, np.float32)
+    assert _dtypes(i64, i64, f32) == (np.int64, np.float32)
+    assert _dtypes(i32, i32, f64) == (np.int32, np.float64)
+    assert _dtypes(i64, i32, f64) == (np.int64, np.float64)
+
+
+def test_builder_needs_a_device_and_rejects_bad_types():
+    from page_rank_gb300 import graph_link as gl
+    A = sp.random(8, 8, density=0.3, format="csr", dtype=np.float32, random_state=0)
+    with pytest.raises(TypeError):
+        gl.csr_to_pbr(A.toarray())
+    with pytest.raises(TypeError):
+        gl.csr_to_pbr(A, min_nnz_per_block=256)
+    if not torch.cuda.is_available():
+        with pytest.raises(RuntimeError):
+            gl.csr_to_pbr(A)
+
+
+def test_cpu_matmul_raises_like_reference():
+    from page_rank_gb300 import graph_link as gl
+    with pytest.raises(TypeError):
+        gl.pbr_batched_matmul_cpu(None, torch.zeros(2, 2))
+
+
+def test_synthetic_generators_are_column_stochastic_and_seeded():
+    from page_rank_gb300 import synth
+    for g in (synth.sbm_graph(8, 16, 0.3, 0.01, seed=1),
+              synth.cluster_rmat_graph(log2n=10, seed=2),
+              synth.cluster_zipf_graph(log2n=10, mean_degree=6.0, seed=3)):
+        cs = np.asarray(g.A.sum(axis=0)).ravel()
+        assert np.allclose(cs[~g.dangling], 1.0, atol=1e-5)
+        assert (cs[g.dangling] == 0).all()
+        assert g.A.has_canonical_format
+    a = synth.cluster_zipf_graph(log2n=10, mean_degree=6.0, seed=3).A
+    b = synth.cluster_zipf_graph(log2n=10, mean_degree=6.0, seed=3).A
+    assert (a != b).nnz == 0
+    sets = synth.seed_sets(100, 10, 1, 32, seed=4)
+    assert all(1 <= len(s) <= 32 and len(np.unique(s)) == len(s) for s in sets)
+
+
+def test_certified_tolerance():
+    from page_rank_gb300.engine import certified_tolerance
+    assert certified_tolerance(1e-6, 0.85) == pytest.approx(1e-6 * 0.15 / 0.85)
