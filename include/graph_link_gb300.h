@@ -61,7 +61,7 @@ int gl_version(void);
  * into pieces of piece_work entries, processed independently and reduced in
  * piece order.  column_tile caps the columns one warp covers (0: automatic).
  * lane_split picks how a warp's lanes share a stripe for 64..127 columns:
- * 0 automatic, 1 all 32 lanes on each nonzero, 2 two half-warps taking
+ * 0 automatic (half-warps for the SpMM), 1 all 32 lanes on each nonzero, 2 two half-warps taking
  * alternate nonzeros (float4 lanes).
  */
 typedef struct gl_pbr_matrix {

@@ -55,14 +55,18 @@ def power_iteration_fp64(A: sp.csr_matrix, V: np.ndarray, alpha: float, max_iter
 
 def direct_solve_fp64(A: sp.csr_matrix, V: np.ndarray, alpha: float,
                       dangling: np.ndarray | None = None) -> np.ndarray:
+    """Fixed point of x = alpha (A + v d^T) x + (1 - alpha) v for every column
+    v of V (d = dangling indicator): one sparse LU of I - alpha A, and the
+    rank-one dangling term per column by Sherman-Morrison."""
     n = A.shape[0]
-    A64 = A.astype(np.float64).tocsc()
-    X = np.zeros_like(V, dtype=np.float64)
-    for k in range(V.shape[1]):
-        v = V[:, k]
-        M = sp.identity(n, format="csc") - alpha * A64
-        if dangling is not None and dangling.any():
-            d = sp.csr_matrix(dangling.astype(np.float64)[None, :])
-            M = M - alpha * sp.csc_matrix(sp.csr_matrix(v[:, None]) @ d)
-        X[:, k] = spla.spsolve(M.tocsc(), (1.0 - alpha) * v)
-    return X
+    M = (sp.identity(n, format="csc") - alpha * A.astype(np.float64).tocsc()).tocsc()
+    lu = spla.splu(M)
+    V = np.asarray(V, dtype=np.float64)
+    Y = lu.solve((1.0 - alpha) * V)
+    if dangling is None or not np.any(dangling):
+        return Y
+    d = np.asarray(dangling, dtype=bool)
+    Z = lu.solve(alpha * V)
+    dy = Y[d].sum(axis=0)
+    dz = Z[d].sum(axis=0)
+    return Y + Z * (dy / (1.0 - dz))[None, :]

@@ -63,31 +63,27 @@ StripeArgs<S> make_args(const gl_pbr_matrix* A) {
     return a;
 }
 
-inline int64_t align256(int64_t x) { return (x + 255) & ~int64_t(255); }
-
-int64_t partial_bytes(const gl_pbr_matrix* A, int64_t batch, int64_t K) {
-    if (A->num_pieces <= 0) return 0;
-    const int64_t elem = A->value_type == GL_F32 ? 4 : 8;
-    const int64_t Kt = ceil_div(K, 128) * 128;
-    return align256((int64_t)A->num_pieces * batch * A->block_rows * Kt * elem);
-}
-
 int64_t workspace_bytes(const gl_pbr_matrix* A, int64_t batch, int64_t K) {
-    if (A->num_pieces <= 0) return 0;
-    return partial_bytes(A, batch, K) + align256((int64_t)A->num_heavy * batch * K * 4);
+    return workspace_layout(A, batch, K).total;
 }
 
-// Points the kernel's partial / counter buffers into the caller's workspace.
+// Points the kernel's scheduler / counter / partial buffers into the
+// caller's workspace.  Without a workspace the launch distributes stripes
+// statically, which is only possible when no stripe is cut into pieces.
 template <typename S>
 int bind_workspace(StripeArgs<S>& a, const gl_pbr_matrix* A, int64_t batch, int64_t K, void* ws,
                    int64_t ws_bytes) {
-    if (a.num_pieces == 0) return GL_OK;
-    const int64_t need = workspace_bytes(A, batch, K);
-    GL_REQUIRE(ws != nullptr && ws_bytes >= need, GL_ERR_WORKSPACE,
-               "SpMM workspace of %lld bytes needed (gl_pbr_spmm_workspace_bytes)", (long long)need);
+    const WorkspaceLayout w = workspace_layout(A, batch, K);
+    if (ws == nullptr && a.num_pieces == 0) {
+        a.sched = nullptr;
+        return GL_OK;
+    }
+    GL_REQUIRE(ws != nullptr && ws_bytes >= w.total, GL_ERR_WORKSPACE,
+               "SpMM workspace of %lld bytes needed (gl_pbr_spmm_workspace_bytes)", (long long)w.total);
     char* base = static_cast<char*>(ws);
-    a.partial = reinterpret_cast<S*>(base);
-    a.counters = reinterpret_cast<int32_t*>(base + partial_bytes(A, batch, K));
+    a.sched = reinterpret_cast<unsigned long long*>(base);
+    a.counters = reinterpret_cast<int32_t*>(base + w.counters);
+    a.partial = reinterpret_cast<S*>(base + w.partial);
     return GL_OK;
 }
 

@@ -8,12 +8,14 @@
 // pool) and passes this library only its input and output buffers, and a
 // latency-critical request loop where a cudaMalloc / cudaFree would stall on
 // a device-wide synchronization.  Such a caller passes X and Y and nothing
-// else; the partial tiles of the heavy-stripe pieces live in g_spmm_scratch
-// below, whose size is fixed at build time.
+// else; the work scheduler and the partial tiles of the heavy-stripe pieces
+// live in g_spmm_scratch below, whose size is fixed at build time.
 //
 // Costs and limits:
 //   * every GPU that loads this library holds GL_SPMM_STATIC_SCRATCH_BYTES
 //     of device memory for g_spmm_scratch until the process exits;
+//   * each call clears the scratch's scheduler and counter words with one
+//     cudaMemsetAsync on the caller's stream before the launch;
 //   * a call whose scratch need (gl_pbr_spmm_workspace_bytes) exceeds that
 //     size is rejected with GL_ERR_WORKSPACE before anything is launched;
 //   * all calls on a device share the one array, which keeps whatever the
@@ -108,31 +110,25 @@ extern "C" int gl_pbr_spmm_static(const gl_pbr_matrix* A, const void* X, void* Y
     GL_REQUIRE(X != nullptr && Y != nullptr, GL_ERR_INVALID_ARGUMENT, "X / Y is NULL");
     GL_REQUIRE(A->stripe_block_ptr && A->remainder_indptr, GL_ERR_INVALID_ARGUMENT,
                "stripe_block_ptr / remainder_indptr are NULL");
-    // Scratch layout (same as gl_pbr_spmm's workspace): partial tiles first,
-    // then one counter per heavy stripe and tile, which must start at zero.
-    const int64_t elem = A->value_type == GL_F32 ? 4 : 8;
-    const int64_t partial = A->num_pieces > 0
-                                ? (((int64_t)A->num_pieces * batch * A->block_rows * ceil_div(features, 128) * 128 *
-                                        elem + 255) & ~int64_t(255))
-                                : 0;
+    // same layout as gl_pbr_spmm's workspace; the scheduler and the counters
+    // are cleared here (a launch that never ran to completion cannot leave
+    // them dirty for the next call)
+    const WorkspaceLayout w = workspace_layout(A, batch, features);
     void* scratch = nullptr;
-    if (A->num_pieces > 0) {
-        int rc = scratch_address(&scratch);
-        if (rc != GL_OK) return rc;
-        GL_CUDA_TRY(cudaMemsetAsync(static_cast<char*>(scratch) + partial, 0, (size_t)(need - partial), stream));
-    }
+    int rc = scratch_address(&scratch);
+    if (rc != GL_OK) return rc;
+    GL_CUDA_TRY(cudaMemsetAsync(scratch, 0, (size_t)w.zero_bytes, stream));
+    char* base = static_cast<char*>(scratch);
     if (A->value_type == GL_F32) {
         StripeArgs<float> a = static_args<float>(A, X, Y, batch, features);
-        if (scratch) {
-            a.partial = static_cast<float*>(scratch);
-            a.counters = reinterpret_cast<int32_t*>(static_cast<char*>(scratch) + partial);
-        }
+        a.sched = reinterpret_cast<unsigned long long*>(base);
+        a.counters = reinterpret_cast<int32_t*>(base + w.counters);
+        a.partial = reinterpret_cast<float*>(base + w.partial);
         return launch_stripe<float, false>(a, A->block_rows, A->block_cols, A->column_tile, A->lane_split, stream);
     }
     StripeArgs<double> a = static_args<double>(A, X, Y, batch, features);
-    if (scratch) {
-        a.partial = static_cast<double*>(scratch);
-        a.counters = reinterpret_cast<int32_t*>(static_cast<char*>(scratch) + partial);
-    }
+    a.sched = reinterpret_cast<unsigned long long*>(base);
+    a.counters = reinterpret_cast<int32_t*>(base + w.counters);
+    a.partial = reinterpret_cast<double*>(base + w.partial);
     return launch_stripe<double, false>(a, A->block_rows, A->block_cols, A->column_tile, A->lane_split, stream);
 }

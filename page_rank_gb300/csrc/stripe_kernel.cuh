@@ -4,19 +4,22 @@
 // for one column tile.  The warp's 32 lanes form C column lanes x P nonzero
 // lanes (C * P = 32): column lane c owns V consecutive columns of the tile
 // (T = C * V columns per tile), and the P nonzero lanes split the stripe's
-// blocks and remainder entries between them.  Each lane keeps
-// block_rows x V accumulators in registers; at the end the P partial sums
-// are folded with warp shuffles and the tile is written once — no atomics on
-// the output, no pre-zeroed output, no second stream.
+// entries between them.  The stripe's output tile [block_rows][T] lives in
+// the warp's shared memory and is written to Y once — no atomics on the
+// output, no pre-zeroed output, no second stream.
 //
-//   * PBR blocks: the lane stages the X rows of the block's active columns
-//     (one vector load each, all issued before use) in its own shared-memory
-//     slots, then walks the set bits of the 64-bit code row by row; values
-//     are packed in row-major bit order, so the value index is a counter.
-//     With P == 1 the warp loads the metadata of 32 blocks at once and
-//     broadcasts it with shuffles.
-//   * CSR remainder: row by row; with P == 1 the warp loads 32 (column,
-//     value) pairs at once and issues the X-row gathers eight at a time.
+//   * P <= 2 (32 or more columns): per chunk of 32 blocks the lanes decode
+//     one block each (metadata in registers, one packed warp scan of the
+//     per-row bit counts) into row-sorted (column, value) lists in shared
+//     memory, followed by each row's CSR-remainder entries; the warp then
+//     walks one row at a time, issuing GL_GATHER_DEPTH X-row gathers before
+//     their FMAs into one V-wide accumulator, and adds the row to the tile.
+//     Values are packed in row-major bit order, so a block's entries of one
+//     row are a contiguous run.
+//   * P > 2 (fewer than 32 columns): the nonzero lanes stride the blocks
+//     (staging the X rows of each block's active columns in shared memory)
+//     and the remainder entries, with block_rows x V accumulators in
+//     registers folded by shuffles into the tile.
 //
 // Load balance: stripes whose stored entries exceed 2 x piece_work (R-MAT
 // hub rows reach tens of thousands) are cut into pieces of piece_work
@@ -41,7 +44,30 @@
 namespace gl {
 
 constexpr int kStripeThreads = 256;
+#ifndef GL_STATIC_PERCENT
+#define GL_STATIC_PERCENT 0
+#endif
 constexpr int kStripeWarps = kStripeThreads / 32;
+
+// Workspace of one SpMM / power-iteration launch (caller-provided or the
+// static scratch): [scheduler: 256 B][heavy-stripe counters][partial tiles].
+// The first zero_bytes must be zero before the first launch; every launch
+// leaves them zero again.
+inline int64_t align256(int64_t x) { return (x + 255) & ~int64_t(255); }
+struct WorkspaceLayout {
+    int64_t counters, partial, zero_bytes, total;
+};
+inline WorkspaceLayout workspace_layout(const gl_pbr_matrix* A, int64_t batch, int64_t K) {
+    WorkspaceLayout w{};
+    const bool heavy = A->num_pieces > 0;
+    const int64_t elem = A->value_type == GL_F32 ? 4 : 8;
+    const int64_t Kt = (K + 127) / 128 * 128;
+    w.counters = 256;
+    w.partial = w.counters + (heavy ? align256((int64_t)A->num_heavy * batch * K * 4) : 0);
+    w.zero_bytes = w.partial;
+    w.total = w.partial + (heavy ? align256((int64_t)A->num_pieces * batch * A->block_rows * Kt * elem) : 0);
+    return w;
+}
 
 template <typename S, int V>
 struct alignas(sizeof(S) * V) Pack {
@@ -70,6 +96,14 @@ struct StripeArgs {
     const int32_t* piece_heavy;    // [num_pieces]
     S* partial;                    // [num_pieces][batch * ntiles][BR][T]
     int32_t* counters;             // [num_heavy][batch * ntiles], zero between calls
+    // work distribution: items [0, static_items) go round-robin over the
+    // warps, the rest are drawn from sched[0] by whichever warp is free;
+    // sched[1] counts retired warps.  Both are zero between calls (the last
+    // warp to retire resets them).  sched == nullptr: all items are static.
+    // (GL_STATIC_PERCENT sets the static share; drawing everything measured
+    // fastest: stripe costs vary too much for any fixed split.)
+    unsigned long long* sched;
+    int64_t static_items;
     // power-iteration epilogue
     const int32_t* tp_ptr;
     const int32_t* tp_row;
@@ -111,59 +145,103 @@ __device__ __forceinline__ int32_t lower_bound_i32(const int32_t* offsets, int32
 }
 
 // ---------------------------------------------------------------------------
-// Accumulation for P == 1 (one warp = one stripe, every lane owns V columns),
-// in two phases per stripe row:
-//   decode  — lanes take one block each (32 blocks per pass, metadata in
-//             registers), extract the block's bits of row r, and write their
-//             (column, value) entries to the warp's list in shared memory at
-//             slots given by a warp prefix sum; the row's remainder entries
-//             are appended lane-parallel after them;
-//   consume — the whole warp walks the row's list: one broadcast shared load
-//             per entry, the X-row gathers issued eight at a time before their
-//             FMAs, accumulators of row r addressed statically.
-// Decoding is lane-parallel (a few instructions per nonzero spread over the
-// warp); consuming costs one load, one address and V FMAs per nonzero.
+// List machinery for P <= 2.  Decoding is lane-parallel (a few instructions
+// per nonzero spread over the warp); consuming costs two broadcast shared
+// loads, one address and V FMAs per nonzero, with the gathers of a batch all
+// in flight before the first FMA.
 // ---------------------------------------------------------------------------
-constexpr int kListCap = 640;     // entries per warp list: a 512-entry unit plus row padding
-// row gathers in flight per warp: enough bytes in flight per SM at moderate
-// register cost (V = 4 moves 512 B per gather)
-template <int V>
+constexpr int kListCap = 384;     // entries per warp list (a unit that does not fit goes row by row)
+// X-row gathers in flight per warp in the main batch (half that for 16-byte
+// lanes); row tails go in batches of kTail
+#ifndef GL_GATHER_DEPTH
+#define GL_GATHER_DEPTH 16
+#endif
+constexpr int kTail = 4;
+template <typename S, int V>
 struct Gather {
-    static constexpr int n = V >= 4 ? 4 : 8;
+    static constexpr int n = sizeof(S) * V >= 16 ? GL_GATHER_DEPTH / 2 : GL_GATHER_DEPTH;
 };
 
-// The list is padded to a multiple of (gather depth x nonzero lanes) with
-// (column 0, value 0) entries, so the loop carries no predicates; lanes past
-// the last column gather from a clamped (valid) address and never store.
-// With P = 2 the two half-warps take alternate entries (each half-warp
-// covers the whole column tile with V-wide loads).
-template <typename S, int V, int P>
-__device__ __forceinline__ void consume_list(S (&t)[V], const int32_t* lcol, const S* lval, int n_padded,
-                                             const S* __restrict__ Xb, int32_t K, int p_lane) {
-    constexpr int NG = Gather<V>::n;
-    for (int e0 = p_lane; e0 < n_padded; e0 += NG * P) {
-        Pack<S, V> x[NG];
+// One list entry: column and value side by side, so one shared load brings
+// both (two FP32 entries per 16-byte load).
+template <typename S>
+struct Entry;
+template <>
+struct alignas(8) Entry<float> {
+    int32_t col;
+    float val;
+};
+template <>
+struct alignas(16) Entry<double> {
+    int32_t col;
+    int32_t pad;
+    double val;
+};
+template <typename S>
+__device__ __forceinline__ Entry<S> make_entry(int32_t col, S val) {
+    Entry<S> e{};
+    e.col = col;
+    e.val = val;
+    return e;
+}
+
+// NB gathers (entries e, e + P, ..., all issued before the first FMA) into
+// the lane's V accumulators.  Lanes past the last column gather from a
+// clamped (valid) address and never store.
+template <typename S, int V, int P, int NB>
+__device__ __forceinline__ void gather_batch(S (&t)[V], const Entry<S>* lst, int e, const S* __restrict__ Xb,
+                                             int32_t K) {
+    Pack<S, V> x[NB];
+    if constexpr (P == 1 && sizeof(S) == 4 && NB % 2 == 0) {
+        // two entries per 16-byte broadcast load; the values are read again
+        // after the gathers instead of holding NB more registers
+        const int4* w = reinterpret_cast<const int4*>(lst + e);
 #pragma unroll
-        for (int q = 0; q < NG; ++q) x[q] = load_pack<S, V>(Xb + (long long)lcol[e0 + q * P] * K);
+        for (int q = 0; q < NB; q += 2) {
+            const int4 c = w[q / 2];
+            x[q] = load_pack<S, V>(Xb + (long long)c.x * K);
+            x[q + 1] = load_pack<S, V>(Xb + (long long)c.z * K);
+        }
 #pragma unroll
-        for (int q = 0; q < NG; ++q) {
-            const S v = lval[e0 + q * P];
+        for (int q = 0; q < NB; q += 2) {
+            const int4 c = w[q / 2];
+#pragma unroll
+            for (int j = 0; j < V; ++j) {
+                t[j] = fma(__int_as_float(c.y), x[q].v[j], t[j]);
+                t[j] = fma(__int_as_float(c.w), x[q + 1].v[j], t[j]);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < NB; ++q) x[q] = load_pack<S, V>(Xb + (long long)lst[e + q * P].col * K);
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            const S v = lst[e + q * P].val;
 #pragma unroll
             for (int j = 0; j < V; ++j) t[j] = fma(v, x[q].v[j], t[j]);
         }
     }
 }
 
-// Pads the list [0, n) with (0, 0) entries up to a multiple of NG * P (never
-// past kListCap, which is a multiple of it); returns the padded length.
+// Walks a list whose length is a multiple of kTail * P (padded with (0, 0)
+// entries): main batches while they fill, then tail batches.  With P = 2 the
+// two half-warps take alternate entries (each half-warp covers the whole
+// column tile with V-wide loads).
 template <typename S, int V, int P>
-__device__ __forceinline__ int pad_list(int32_t* lcol, S* lval, int n, int lane) {
-    constexpr int NGP = Gather<V>::n * P;
-    const int np = (n + NGP - 1) / NGP * NGP;
-    if (lane < np - n) {
-        lcol[n + lane] = 0;
-        lval[n + lane] = S(0);
-    }
+__device__ __forceinline__ void consume_list(S (&t)[V], const Entry<S>* lst, int n_padded,
+                                             const S* __restrict__ Xb, int32_t K, int p_lane) {
+    constexpr int NG = Gather<S, V>::n;
+    int e = p_lane;
+    for (; e + (NG - 1) * P < n_padded; e += NG * P) gather_batch<S, V, P, NG>(t, lst, e, Xb, K);
+    for (; e < n_padded; e += kTail * P) gather_batch<S, V, P, kTail>(t, lst, e, Xb, K);
+}
+
+// Pads the list [0, n) with (0, 0) entries up to a multiple of GR (never
+// past kListCap, which is a multiple of it); returns the padded length.
+template <typename S, int GR>
+__device__ __forceinline__ int pad_list(Entry<S>* lst, int n, int lane) {
+    const int np = (n + GR - 1) / GR * GR;
+    if (lane < np - n) lst[n + lane] = make_entry<S>(0, S(0));
     __syncwarp();
     return np;
 }
@@ -180,26 +258,58 @@ struct RowPack {
     }
     __device__ __forceinline__ void set(int r, uint32_t v) { w[r >> 2] |= (uint64_t)v << (16 * (r & 3)); }
     __device__ __forceinline__ uint32_t get(int r) const { return (uint32_t)(w[r >> 2] >> (16 * (r & 3))) & 0xffffu; }
+    // r not known at compile time: select the word without indexing registers
+    __device__ __forceinline__ uint32_t get_dyn(int r) const {
+        uint64_t x = w[0];
+#pragma unroll
+        for (int i = 1; i < W; ++i)
+            if ((r >> 2) == i) x = w[i];
+        return (uint32_t)(x >> (16 * (r & 3))) & 0xffffu;
+    }
 };
 
+// Adds the lane's accumulators to row r of the tile (lane-owned columns)
+// and clears them.
+template <typename S, int V>
+__device__ __forceinline__ void commit_row(S* tile_lane, int r, int T, S (&t)[V], bool own) {
+    if (own) {
+        Pack<S, V>* tp = reinterpret_cast<Pack<S, V>*>(tile_lane + r * T);
+        Pack<S, V> o = *tp;
+#pragma unroll
+        for (int j = 0; j < V; ++j) o.v[j] += t[j];
+        *tp = o;
+    }
+#pragma unroll
+    for (int j = 0; j < V; ++j) t[j] = S(0);
+}
+
+// Accumulation for P <= 2 into the warp's output tile in shared memory
+// (tile[r * T + column], zeroed here, each lane its own columns).  Per chunk
+// of 32 blocks: one packed warp scan of the per-row bit counts; if the
+// chunk's rows (block entries + remainder entries) fit the list, every lane
+// writes its block's entries for all rows at once, row-sorted, otherwise
+// row by row (at most 32 x BC block entries per row, the remainder in
+// list-sized pieces).  The rows are consumed one at a time (each padded to
+// kTail * P entries) into a V-wide accumulator per lane; with P == 2 the two
+// half-warps take alternate entries and are folded by one shuffle per row.
 template <typename S, int BR, int BC, int V, int P>
-__device__ __forceinline__ void accumulate_lists(const StripeArgs<S>& a, S (&acc)[BR][V], unsigned char* smem_raw,
-                                                 int64_t s, int32_t b0, int32_t b1, int32_t j0, int32_t j1,
-                                                 const S* __restrict__ Xb, bool lane_ok, int lane, int p_lane) {
+__device__ __forceinline__ void accumulate_rows(const StripeArgs<S>& a, S* tile, Entry<S>* lst, int32_t* rowinfo,
+                                                int64_t s, int32_t b0, int32_t b1, int32_t j0, int32_t j1,
+                                                const S* __restrict__ Xb, bool lane_ok, int lane, int p_lane,
+                                                int c_lane) {
     constexpr uint32_t ROWMASK = (BC >= 32) ? 0xffffffffu : ((1u << BC) - 1u);
-    constexpr int NG = Gather<V>::n * P;   // list granule: every nonzero lane gets full gather batches
-    const int warp = threadIdx.x >> 5;
-    int32_t* lcol = reinterpret_cast<int32_t*>(smem_raw) + warp * kListCap;
-    S* lval = reinterpret_cast<S*>(smem_raw + (size_t)kStripeWarps * kListCap * sizeof(int32_t)) + warp * kListCap;
-    // per-row bookkeeping of this warp: [rstart | rlen | seg | blen] x BR
-    int32_t* rowinfo = reinterpret_cast<int32_t*>(smem_raw + (size_t)kStripeWarps * kListCap *
-                                                                 (sizeof(int32_t) + sizeof(S))) + warp * 4 * BR;
+    constexpr int GR = kTail * P;   // row granule
+    constexpr int T = (32 / P) * V;
+    static_assert(kListCap % GR == 0 && kListCap >= 32 * BC + 2 * GR, "a row of one block chunk must fit the list");
     int32_t* rstart = rowinfo;
     int32_t* rlen = rowinfo + BR;
     int32_t* seg = rowinfo + 2 * BR;
     int32_t* blen = rowinfo + 3 * BR;
+    const bool own = (p_lane == 0) && lane_ok;
+    S* tile_lane = tile + c_lane * V;
 
-    // remainder row ranges of this unit (lane r computes row r)
+    // remainder row ranges of this unit (lane r computes row r); zero the tile
+    __syncwarp();
     if (lane < BR) {
         const int64_t row = s * BR + lane;
         int32_t rs = j1, re = j1;
@@ -212,6 +322,13 @@ __device__ __forceinline__ void accumulate_lists(const StripeArgs<S>& a, S (&acc
         }
         rstart[lane] = rs;
         rlen[lane] = re - rs;
+    }
+    if (own) {
+        Pack<S, V> z;
+#pragma unroll
+        for (int j = 0; j < V; ++j) z.v[j] = S(0);
+#pragma unroll
+        for (int r = 0; r < BR; ++r) store_pack<S, V>(tile_lane + r * T, z);
     }
     __syncwarp();
 
@@ -243,14 +360,14 @@ __device__ __forceinline__ void accumulate_lists(const StripeArgs<S>& a, S (&acc
             const uint64_t t = __shfl_sync(0xffffffffu, v, 31);
             if ((lane >> 2) == i) tot_lane = t;
         }
-        // row segments [block entries | remainder entries | padding]:
+        // row segments [block entries | remainder entries | row padding]:
         // lane r < BR owns row r; a scan over those lanes places them
         int32_t my_len = 0, my_blen = 0;
         if (lane < BR) {
             my_blen = (int32_t)((tot_lane >> (16 * (lane & 3))) & 0xffffu);
             my_len = my_blen + (last ? rlen[lane] : 0);
         }
-        const int32_t padded = (my_len + NG - 1) / NG * NG;
+        const int32_t padded = (my_len + GR - 1) / GR * GR;
         const int32_t incl_pad = (int32_t)warp_incl_scan_i64(padded);
         const int32_t total = __shfl_sync(0xffffffffu, incl_pad, BR - 1);
         if (lane < BR) {
@@ -258,7 +375,8 @@ __device__ __forceinline__ void accumulate_lists(const StripeArgs<S>& a, S (&acc
             blen[lane] = my_blen;
         }
         __syncwarp();
-        if (total <= kListCap) {
+        const bool fits = total <= kListCap;
+        if (fits) {
             // this lane's block entries into its rows' segments
             if (code) {
                 int32_t k = off;
@@ -269,9 +387,7 @@ __device__ __forceinline__ void accumulate_lists(const StripeArgs<S>& a, S (&acc
                     while (rb) {
                         const int c = __ffs(rb) - 1;
                         rb &= rb - 1u;
-                        lcol[pos] = col0 + c;
-                        lval[pos] = a.bdata[k++];
-                        ++pos;
+                        lst[pos++] = make_entry<S>(col0 + c, a.bdata[k++]);
                     }
                 }
             }
@@ -281,107 +397,108 @@ __device__ __forceinline__ void accumulate_lists(const StripeArgs<S>& a, S (&acc
                 const int32_t sg = seg[r], bl = blen[r];
                 const int32_t rl = last ? rlen[r] : 0;
                 const int32_t rs = rstart[r];
-                for (int q = lane; q < rl; q += 32) {
-                    lcol[sg + bl + q] = a.rem_col[rs + q];
-                    lval[sg + bl + q] = a.rem_val[rs + q];
-                }
+                for (int q = lane; q < rl; q += 32) lst[sg + bl + q] = make_entry<S>(a.rem_col[rs + q], a.rem_val[rs + q]);
                 const int32_t len = bl + rl;
-                const int32_t pad = (len + NG - 1) / NG * NG - len;
-                if (lane < pad) {
-                    lcol[sg + len + lane] = 0;
-                    lval[sg + len + lane] = S(0);
-                }
+                const int32_t pad = (len + GR - 1) / GR * GR - len;
+                if (lane < pad) lst[sg + len + lane] = make_entry<S>(0, S(0));
             }
             __syncwarp();
-#pragma unroll
-            for (int r = 0; r < BR; ++r) {
-                const int32_t len = blen[r] + (last ? rlen[r] : 0);
-                consume_list<S, V, P>(acc[r], lcol + seg[r], lval + seg[r], (len + NG - 1) / NG * NG, Xb, a.K,
-                                      p_lane);
-            }
-            __syncwarp();
-        } else {
-            // too many entries for one list: one row at a time, remainder in
-            // list-sized pieces
+        }
 #pragma unroll 1
-            for (int r = 0; r < BR; ++r) {
-                S t[V];
+        for (int r = 0; r < BR; ++r) {
+            S t[V];
 #pragma unroll
-                for (int j = 0; j < V; ++j) t[j] = S(0);
+            for (int j = 0; j < V; ++j) t[j] = S(0);
+            int base = 0, n;
+            int32_t rs = 0, re = 0;   // remainder entries still to append (!fits)
+            if (fits) {
+                base = seg[r];
+                n = (blen[r] + (last ? rlen[r] : 0) + GR - 1) / GR * GR;
+            } else {
                 uint32_t rb = (uint32_t)(code >> (r * BC)) & ROWMASK;
                 if (rb) {
-                    int pos = (int)(incl.get(r) - cnt.get(r));
+                    int pos = (int)(incl.get_dyn(r) - cnt.get_dyn(r));
                     int32_t k = off + (r == 0 ? 0 : __popcll(code & ((1ull << (r * BC)) - 1ull)));
                     while (rb) {
                         const int c = __ffs(rb) - 1;
                         rb &= rb - 1u;
-                        lcol[pos] = col0 + c;
-                        lval[pos] = a.bdata[k++];
-                        ++pos;
+                        lst[pos++] = make_entry<S>(col0 + c, a.bdata[k++]);
                     }
                 }
-                int n = blen[r];
+                n = blen[r];
                 if (last) {
-                    int32_t rs = rstart[r];
-                    const int32_t re = rstart[r] + rlen[r];
-                    while (rs < re) {
-                        const int room = kListCap - NG - n;
-                        const int take = (re - rs) < room ? (re - rs) : room;
-                        __syncwarp();
-                        for (int q = lane; q < take; q += 32) {
-                            lcol[n + q] = a.rem_col[rs + q];
-                            lval[n + q] = a.rem_val[rs + q];
-                        }
-                        __syncwarp();
-                        n += take;
-                        rs += take;
-                        if (rs < re) {
-                            consume_list<S, V, P>(t, lcol, lval, pad_list<S, V, P>(lcol, lval, n, lane), Xb,
-                                                  a.K, p_lane);
-                            __syncwarp();
-                            n = 0;
-                        }
-                    }
+                    rs = rstart[r];
+                    re = rs + rlen[r];
                 }
-                __syncwarp();
-                consume_list<S, V, P>(t, lcol, lval, pad_list<S, V, P>(lcol, lval, n, lane), Xb, a.K, p_lane);
-                __syncwarp();
-#pragma unroll
-                for (int rr = 0; rr < BR; ++rr)
-                    if (rr == r) {
-#pragma unroll
-                        for (int j = 0; j < V; ++j) acc[rr][j] += t[j];
-                    }
             }
+            while (true) {
+                if (!fits) {
+                    __syncwarp();
+                    const int room = kListCap - GR - n;
+                    const int take = (re - rs) < room ? (re - rs) : room;
+                    for (int q = lane; q < take; q += 32) lst[n + q] = make_entry<S>(a.rem_col[rs + q], a.rem_val[rs + q]);
+                    n += take;
+                    rs += take;
+                    n = pad_list<S, GR>(lst, n, lane);
+                }
+                consume_list<S, V, P>(t, lst + base, n, Xb, a.K, p_lane);
+                if (rs >= re) break;
+                __syncwarp();
+                n = 0;
+            }
+            if constexpr (P == 2) {
+#pragma unroll
+                for (int j = 0; j < V; ++j) t[j] += __shfl_xor_sync(0xffffffffu, t[j], 16);
+            }
+            commit_row<S, V>(tile_lane, r, T, t, own);
+            if (!fits) __syncwarp();   // the next row reuses the list
         }
+        __syncwarp();
         if (kc >= b1) break;   // empty block range: one pass for the remainder
     }
 }
 
-// Dynamic shared memory of one CTA of stripe_kernel.
-template <typename S, int BC, int V, int C>
-constexpr size_t stripe_smem_bytes() {
-    return (32 / C <= 2) ? (size_t)kStripeWarps * kListCap * (sizeof(int32_t) + sizeof(S)) +
-                               (size_t)kStripeWarps * 4 * BC * sizeof(int32_t)
-                         : (size_t)BC * kStripeThreads * V * sizeof(S);
-}
+// Dynamic shared memory of one CTA of stripe_kernel, per warp: the output
+// tile [BR][T] (offset 0), then for P <= 2 the (column, value) list and the
+// row bookkeeping, or for P > 2 the staged X rows of one block per lane.
+template <typename S, int BR, int V, int C>
+struct StripeSmem {
+    static constexpr int P = 32 / C;
+    static constexpr int T = C * V;
+    static constexpr size_t tile = (size_t)kStripeWarps * BR * T * sizeof(S);
+    static constexpr size_t list = P <= 2 ? (size_t)kStripeWarps * kListCap * sizeof(Entry<S>) : 0;
+    static constexpr size_t info = P <= 2 ? (size_t)kStripeWarps * 4 * BR * sizeof(int32_t) : 0;
+    static constexpr size_t stage = P > 2 ? (size_t)BR * kStripeThreads * V * sizeof(S) : 0;
+    static constexpr size_t bytes = tile + list + info + stage;
+    static_assert(tile % 16 == 0 && list % 16 == 0, "regions stay 16-byte aligned");
+};
 
-// Minimum resident CTAs per SM the register allocation must allow.
-// (the power-iteration epilogue needs more registers than the plain store)
-template <int V, bool PPR, int C>
+// Minimum resident CTAs per SM the register allocation must allow (64
+// registers per thread at 4; the power-iteration epilogue with 16-byte lanes
+// needs more).
+#ifndef GL_STRIPE_MIN_CTAS
+#define GL_STRIPE_MIN_CTAS 4
+#endif
+template <typename S, int V, bool PPR>
 struct MinBlocks {
-    static constexpr int n = (V >= 4 && C == 32) ? 2 : (PPR || V >= 4 ? 3 : 4);
+    static constexpr int n = (PPR && sizeof(S) * V >= 16) ? 3 : GL_STRIPE_MIN_CTAS;
 };
 
 template <typename S, int BR, int BC, int V, int C, bool PPR>
-__global__ void __launch_bounds__(kStripeThreads, MinBlocks<V, PPR, C>::n)
+__global__ void __launch_bounds__(kStripeThreads, MinBlocks<S, V, PPR>::n)
 stripe_kernel(const StripeArgs<S> a) {
     constexpr int P = 32 / C;            // nonzero lanes per warp
     constexpr int T = C * V;             // columns per tile
     constexpr uint32_t ROWMASK = (BC >= 32) ? 0xffffffffu : ((1u << BC) - 1u);
 
+    using SM = StripeSmem<S, BR, V, C>;
     extern __shared__ __align__(16) unsigned char xs_dyn[];
     __shared__ int s_skip;
+    const int warp = threadIdx.x >> 5;
+    S* const otile = reinterpret_cast<S*>(xs_dyn) + (size_t)warp * BR * T;
+    Entry<S>* const lst = reinterpret_cast<Entry<S>*>(xs_dyn + SM::tile) + (size_t)warp * kListCap;
+    int32_t* const rowinfo = reinterpret_cast<int32_t*>(xs_dyn + SM::tile + SM::list) + (size_t)warp * 4 * BR;
+    Pack<S, V>* const xstage = reinterpret_cast<Pack<S, V>*>(xs_dyn + SM::tile);
 
     const int lane = threadIdx.x & 31;
     const int c_lane = lane % C;
@@ -444,7 +561,22 @@ stripe_kernel(const StripeArgs<S> a) {
         }
     };
 
-    for (int64_t item = warp_id; item < items; item += nwarps) {
+    // next work item: static round-robin first, then drawn from the counter
+    bool drawing = warp_id >= a.static_items;
+    auto draw = [&]() -> int64_t {
+        unsigned long long v = 0;
+        if (lane == 0) v = atomicAdd(a.sched, 1ull);
+        return a.static_items + (int64_t)__shfl_sync(0xffffffffu, v, 0);
+    };
+    auto next_item = [&](int64_t cur) -> int64_t {
+        if (!drawing) {
+            if (cur + nwarps < a.static_items) return cur + nwarps;
+            if (a.sched == nullptr) return items;
+            drawing = true;
+        }
+        return draw();
+    };
+    for (int64_t item = drawing ? (a.sched ? draw() : items) : warp_id; item < items; item = next_item(item)) {
         const int64_t u = item / BT;
         const int64_t bt = item - u * BT;
         const int64_t b = bt / a.ntiles;
@@ -512,18 +644,18 @@ stripe_kernel(const StripeArgs<S> a) {
             }
         }
 
-        S acc[BR][V];
-#pragma unroll
-        for (int r = 0; r < BR; ++r)
-#pragma unroll
-            for (int j = 0; j < V; ++j) acc[r][j] = S(0);
-
         // lanes past the last column read a valid address and never store
         const S* __restrict__ Xb = a.X + b * a.cols * (int64_t)a.K + (lane_ok ? col_base : 0);
 
         if constexpr (P <= 2) {
-            accumulate_lists<S, BR, BC, V, P>(a, acc, xs_dyn, s, b0, b1, j0, j1, Xb, lane_ok, lane, p_lane);
+            accumulate_rows<S, BR, BC, V, P>(a, otile, lst, rowinfo, s, b0, b1, j0, j1, Xb, lane_ok, lane,
+                                             p_lane, c_lane);
         } else {
+            S acc[BR][V];
+#pragma unroll
+            for (int r = 0; r < BR; ++r)
+#pragma unroll
+                for (int j = 0; j < V; ++j) acc[r][j] = S(0);
             // ---- PBR blocks: lanes stride the blocks ------------------------
             for (int32_t kb = b0 + p_lane; kb < b1; kb += P) {
                 const uint64_t code = static_cast<uint64_t>(a.codes[kb]);
@@ -532,12 +664,11 @@ stripe_kernel(const StripeArgs<S> a) {
                 uint32_t colmask = 0;
 #pragma unroll
                 for (int r = 0; r < BR; ++r) colmask |= (uint32_t)(code >> (r * BC)) & ROWMASK;
-                Pack<S, V>* xs = reinterpret_cast<Pack<S, V>*>(xs_dyn);
                 if (lane_ok) {
 #pragma unroll
                     for (int c = 0; c < BC; ++c)
                         if ((colmask >> c) & 1u)
-                            xs[c * kStripeThreads + threadIdx.x] = load_pack<S, V>(Xb + (col0 + c) * a.K);
+                            xstage[c * kStripeThreads + threadIdx.x] = load_pack<S, V>(Xb + (col0 + c) * a.K);
                 }
 #pragma unroll
                 for (int r = 0; r < BR; ++r) {
@@ -547,7 +678,7 @@ stripe_kernel(const StripeArgs<S> a) {
                         bits &= bits - 1u;
                         const S v = a.bdata[k++];
                         if (lane_ok) {
-                            const Pack<S, V> x = xs[c * kStripeThreads + threadIdx.x];
+                            const Pack<S, V> x = xstage[c * kStripeThreads + threadIdx.x];
 #pragma unroll
                             for (int j = 0; j < V; ++j) acc[r][j] = fma(v, x.v[j], acc[r][j]);
                         }
@@ -592,29 +723,33 @@ stripe_kernel(const StripeArgs<S> a) {
                     }
                 }
             }
-        }
-
-        // ---- fold the P nonzero lanes ----------------------------------------
-        if constexpr (P > 1) {
+            // ---- fold the P nonzero lanes into the tile ------------------------
 #pragma unroll
             for (int off = C; off < 32; off <<= 1)
 #pragma unroll
                 for (int r = 0; r < BR; ++r)
 #pragma unroll
                     for (int j = 0; j < V; ++j) acc[r][j] += __shfl_xor_sync(0xffffffffu, acc[r][j], off);
-        }
-
-        // ---- heavy stripe: publish the partial; the last piece reduces ------
-        if (h >= 0) {
-            S* part = a.partial + ((int64_t)u * BT + bt) * BR * T + c_lane * V;
             if (p_lane == 0 && lane_ok) {
 #pragma unroll
                 for (int r = 0; r < BR; ++r) {
                     Pack<S, V> o;
 #pragma unroll
                     for (int j = 0; j < V; ++j) o.v[j] = acc[r][j];
-                    store_pack<S, V>(part + r * T, o);
+                    store_pack<S, V>(otile + r * T + c_lane * V, o);
                 }
+            }
+        }
+        // from here on lane (c_lane, p_lane == 0) owns columns [c_lane * V, +V)
+        // of every tile row
+
+        // ---- heavy stripe: publish the partial; the last piece reduces ------
+        if (h >= 0) {
+            S* part = a.partial + ((int64_t)u * BT + bt) * BR * T + c_lane * V;
+            if (p_lane == 0 && lane_ok) {
+#pragma unroll 2
+                for (int r = 0; r < BR; ++r)
+                    store_pack<S, V>(part + r * T, load_pack<S, V>(otile + r * T + c_lane * V));
             }
             __threadfence();
             __syncwarp();
@@ -628,78 +763,89 @@ stripe_kernel(const StripeArgs<S> a) {
             if (!last) continue;
             __threadfence();
             const int64_t first = (int64_t)a.heavy_first[h];
-#pragma unroll
-            for (int r = 0; r < BR; ++r)
-#pragma unroll
-                for (int j = 0; j < V; ++j) acc[r][j] = S(0);
             if (p_lane == 0 && lane_ok) {
-                for (int32_t q = 0; q < npieces; ++q) {
-                    const S* pp = a.partial + ((first + q) * BT + bt) * BR * T + c_lane * V;
+#pragma unroll 1
+                for (int r = 0; r < BR; ++r) {
+                    Pack<S, V> o;
 #pragma unroll
-                    for (int r = 0; r < BR; ++r) {
-                        const Pack<S, V> x = load_pack_cg<S, V>(pp + r * T);
+                    for (int j = 0; j < V; ++j) o.v[j] = S(0);
+                    for (int32_t q = 0; q < npieces; ++q) {
+                        const Pack<S, V> x =
+                            load_pack_cg<S, V>(a.partial + ((first + q) * BT + bt) * BR * T + c_lane * V + r * T);
 #pragma unroll
-                        for (int j = 0; j < V; ++j) acc[r][j] += x.v[j];
+                        for (int j = 0; j < V; ++j) o.v[j] += x.v[j];
                     }
+                    store_pack<S, V>(otile + r * T + c_lane * V, o);
                 }
             }
         }
 
-        if (!(lane_ok && p_lane == 0)) continue;
+        if (lane_ok && p_lane == 0) {
+            const S* trow = otile + c_lane * V;
 
-        // ---- epilogue --------------------------------------------------------
-        if constexpr (!PPR) {
-            S* Yb = a.Y + (b * a.rows) * (int64_t)a.K + col_base;
-#pragma unroll
-            for (int r = 0; r < BR; ++r) {
-                const int64_t row = s * BR + r;
-                if (row < a.rows) {
-                    Pack<S, V> o;
-#pragma unroll
-                    for (int j = 0; j < V; ++j) o.v[j] = acc[r][j];
-                    store_pack<S, V>(Yb + row * a.K, o);
+            // ---- epilogue --------------------------------------------------------
+            if constexpr (!PPR) {
+                S* Yb = a.Y + (b * a.rows) * (int64_t)a.K + col_base;
+#pragma unroll 2
+                for (int r = 0; r < BR; ++r) {
+                    const int64_t row = s * BR + r;
+                    if (row < a.rows) store_pack<S, V>(Yb + row * a.K, load_pack<S, V>(trow + r * T));
                 }
-            }
-        } else {
+            } else {
+                S* tw = otile + c_lane * V;
+#pragma unroll 2
+                for (int r = 0; r < BR; ++r) {
+                    Pack<S, V> o = load_pack<S, V>(tw + r * T);
 #pragma unroll
-            for (int r = 0; r < BR; ++r)
-#pragma unroll
-                for (int j = 0; j < V; ++j) acc[r][j] = fma(alpha, acc[r][j], unif[j]);
-            const int32_t e0 = a.tp_ptr[s], e1 = a.tp_ptr[s + 1];
-            for (int32_t e = e0; e < e1; ++e) {
-                const int rr = a.tp_row[e] - (int)(s * BR);
-                const int cc = a.tp_col[e] - col_base;
-                if (cc >= 0 && cc < V) {
-                    const S w = static_cast<S>(a.tp_w[e]);
-#pragma unroll
-                    for (int r = 0; r < BR; ++r)
-#pragma unroll
-                        for (int j = 0; j < V; ++j)
-                            if (r == rr && j == cc) acc[r][j] = fma(w, scale[j], acc[r][j]);
+                    for (int j = 0; j < V; ++j) o.v[j] = fma(alpha, o.v[j], unif[j]);
+                    store_pack<S, V>(tw + r * T, o);
                 }
-            }
-            const S* Xin = a.X + col_base;
-            S* Xout = a.Y + col_base;
+                const int32_t e0 = a.tp_ptr[s], e1 = a.tp_ptr[s + 1];
+                for (int32_t e = e0; e < e1; ++e) {
+                    const int rr = a.tp_row[e] - (int)(s * BR);
+                    const int cc = a.tp_col[e] - col_base;
+                    if (cc >= 0 && cc < V) {
+                        S sc = scale[0];
 #pragma unroll
-            for (int r = 0; r < BR; ++r) {
-                const int64_t row = s * BR + r;
-                if (row < a.rows) {
-                    const Pack<S, V> old = load_pack<S, V>(Xin + row * a.K);
-                    const bool dang = a.dbitmap != nullptr && ((a.dbitmap[row >> 5] >> (row & 31)) & 1u);
-                    Pack<S, V> o;
-#pragma unroll
-                    for (int j = 0; j < V; ++j) {
-                        const S nv = frozen[j] ? old.v[j] : acc[r][j];
-                        o.v[j] = nv;
-                        res_acc[j] += (float)fabs(nv - old.v[j]);
-                        if (dang) dang_acc[j] += (float)nv;
+                        for (int j = 1; j < V; ++j)
+                            if (j == cc) sc = scale[j];
+                        tw[rr * T + cc] = fma(static_cast<S>(a.tp_w[e]), sc, tw[rr * T + cc]);
                     }
-                    store_pack<S, V>(Xout + row * a.K, o);
+                }
+                const S* Xin = a.X + col_base;
+                S* Xout = a.Y + col_base;
+#pragma unroll 2
+                for (int r = 0; r < BR; ++r) {
+                    const int64_t row = s * BR + r;
+                    if (row < a.rows) {
+                        const Pack<S, V> old = load_pack<S, V>(Xin + row * a.K);
+                        const Pack<S, V> y = load_pack<S, V>(tw + r * T);
+                        const bool dang = a.dbitmap != nullptr && ((a.dbitmap[row >> 5] >> (row & 31)) & 1u);
+                        Pack<S, V> o;
+#pragma unroll
+                        for (int j = 0; j < V; ++j) {
+                            const S nv = frozen[j] ? old.v[j] : y.v[j];
+                            o.v[j] = nv;
+                            res_acc[j] += (float)fabs(nv - old.v[j]);
+                            if (dang) dang_acc[j] += (float)nv;
+                        }
+                        store_pack<S, V>(Xout + row * a.K, o);
+                    }
                 }
             }
         }
     }
     flush();
+    if (a.sched != nullptr && lane == 0) {
+        // this warp draws nothing more; the last one to retire resets the
+        // scheduler for the next launch (nobody waits on anybody)
+        __threadfence();
+        if (atomicAdd(a.sched + 1, 1ull) == (unsigned long long)nwarps - 1) {
+            a.sched[0] = 0;
+            a.sched[1] = 0;
+            __threadfence();
+        }
+    }
 }
 
 // Host-side launcher for one (S, PPR) family; picks the block shape, the

@@ -15,7 +15,7 @@ int launch_stripe_shape(const StripeArgs<S>& a0, cudaStream_t stream) {
     const int64_t items = units * a.batch * (int64_t)a.ntiles;
     if (items == 0) return GL_OK;
     auto kern = stripe_kernel<S, BR, BR, V, C, PPR>;
-    constexpr size_t smem = stripe_smem_bytes<S, BR, V, C>();
+    constexpr size_t smem = StripeSmem<S, BR, V, C>::bytes;
     static int occ = 0;
     if (occ == 0) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -26,6 +26,9 @@ int launch_stripe_shape(const StripeArgs<S>& a0, cudaStream_t stream) {
     int64_t blocks = ceil_div(items, kStripeWarps);
     const int64_t cap = (int64_t)num_sms() * occ;
     if (blocks > cap) blocks = cap;
+    // the first GL_STATIC_PERCENT % of the items (whole rounds) go round-robin
+    const int64_t nwarps = blocks * kStripeWarps;
+    a.static_items = a.sched ? items * GL_STATIC_PERCENT / 100 / nwarps * nwarps : items;
     kern<<<(unsigned)blocks, kStripeThreads, smem, stream>>>(a);
     GL_LAUNCH_CHECK("stripe_kernel");
     return GL_OK;
@@ -49,8 +52,9 @@ Shape pick_shape(int64_t K, int tile_hint, const void* X, const void* Y, bool al
     int cap = tile_hint > 0 ? tile_hint : 1 << 30;
     if (sizeof(S) == 8 && K < 17) return {1, 1};   // FP64 instantiates only C = 1 below 17 columns
     // 64 <= K < 128 (FP32): two half-warps with float4 lanes each cover 64
-    // columns and take alternate nonzeros
-    if (allow_half_warps && lane_split == 2 && sizeof(S) == 4 && K >= 64 && K < 128 && 64 <= cap && vec_ok(4))
+    // columns and take alternate nonzeros (the default; lane_split 1 keeps
+    // all 32 lanes on each nonzero)
+    if (allow_half_warps && lane_split != 1 && sizeof(S) == 4 && K >= 64 && K < 128 && 64 <= cap && vec_ok(4))
         return {4, 16};
     if (K >= 32) {
         for (int v = max_v; v >= 1; v >>= 1)

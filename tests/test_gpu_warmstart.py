@@ -90,7 +90,9 @@ def test_trained_warm_start_gains_iterations(device):
     warm = ws.solve(sets, tol=1e-6)
     assert cold.converged.all() and warm.converged.all()
     assert warm.iterations.sum() < cold.iterations.sum()
-    X64 = oppr.direct_solve_fp64(g.A, oppr.teleport_matrix(g.n, sets), 0.85, g.dangling)
+    # FP64 fixed point by power iteration to 1e-14 (a sparse LU of this hub graph fills in)
+    X64, _, ok, _ = oppr.power_iteration_fp64(g.A, oppr.teleport_matrix(g.n, sets), 0.85, 5000, 1e-14, g.dangling)
+    assert ok
     for res in (cold, warm):
         l1 = np.abs(res.X.cpu().numpy().astype(np.float64) - X64).sum(axis=0)
         assert l1.max() <= 1e-6
