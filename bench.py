@@ -60,7 +60,7 @@ def measured_peak():
 
 def profile_traffic(nb_scale_bytes: int):
     """DRAM bytes per launch from the committed ncu summary of this workload."""
-    p = ROOT / "profiles" / "spmm_stripe_kernel_rmat2e20_f64.md"
+    p = ROOT / "profiles" / "stripe_kernel_spmm_rmat2e20_64cols.md"
     if not p.is_file():
         return None
     for line in p.read_text().splitlines():

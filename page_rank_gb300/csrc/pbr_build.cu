@@ -77,6 +77,11 @@ struct BuildWs {
                             // (rec_tau later holds the output slot, -1 = dropped)
     int32_t*  rec_pos;      // list position
     int32_t*  rec_pops;     // popcount of the block code
+    // big stripes: sort / scan scratch (same indexing)
+    int32_t*  rec_k0;
+    int32_t*  rec_v0;
+    int32_t*  rec_k1;
+    int32_t*  rec_v1;
     int64_t bytes;
 };
 
@@ -106,6 +111,10 @@ BuildWs layout_ws(void* base, int64_t rows, int64_t nnz, int32_t br) {
     w.rec_g = reinterpret_cast<int32_t*>(take(4 * nr));
     w.rec_pos = reinterpret_cast<int32_t*>(take(4 * nr));
     w.rec_pops = reinterpret_cast<int32_t*>(take(4 * nr));
+    w.rec_k0 = reinterpret_cast<int32_t*>(take(4 * nr));
+    w.rec_v0 = reinterpret_cast<int32_t*>(take(4 * nr));
+    w.rec_k1 = reinterpret_cast<int32_t*>(take(4 * nr));
+    w.rec_v1 = reinterpret_cast<int32_t*>(take(4 * nr));
     w.bytes = off;
     return w;
 }
@@ -241,9 +250,9 @@ __device__ __forceinline__ uint32_t key_bucket(int64_t key_value, bool key32, ui
     return (uint32_t)((uint64_t)k % buckets);
 }
 
-// A team is the set of threads that orders one stripe: a warp for stripes
-// with few distinct blocks, a whole 1024-thread CTA for big ones (R-MAT hub
-// rows put tens of thousands of blocks into one stripe).
+// A team is the set of threads that orders one stripe with order_stripe: a
+// warp, for stripes with up to kSmallStripeBlocks distinct blocks (bigger
+// ones go through order_stripe_big).
 template <int TEAM>
 struct Team;
 template <>
@@ -251,15 +260,9 @@ struct Team<32> {
     static __device__ __forceinline__ int rank() { return threadIdx.x & 31; }
     static __device__ __forceinline__ void sync() { __syncwarp(); }
 };
-template <>
-struct Team<1024> {
-    static __device__ __forceinline__ int rank() { return threadIdx.x; }
-    static __device__ __forceinline__ void sync() { __syncthreads(); }
-};
 
 constexpr int kSmallStripeBlocks = 64;   // warp team up to this many distinct blocks
 constexpr int kBigThreads = 1024;
-constexpr int kBigStage = 1536;          // big stripes up to this size are staged in shared memory
 
 // Orders the records with insertion rank < present as the standard library's
 // node list would under `buckets` (see the file comment); writes list
@@ -349,6 +352,253 @@ __device__ void move_values(const I* indptr, const I* indices, const S* values, 
         }
         ++j;
     }
+}
+
+// ---------------------------------------------------------------------------
+// Big stripes (more than kSmallStripeBlocks distinct blocks; R-MAT hub rows
+// reach 17 k blocks in one stripe of the 2^20 graph): the same emit order,
+// computed by one 1024-thread CTA in O(m) passes over global scratch instead
+// of the warp path's O(m^2) comparisons:
+//   * insertion ranks: a stable radix sort of the first CSR positions;
+//   * per rehash phase: the participating records in insertion-rank order
+//     (a scatter: the ranks are a permutation), a stable radix sort of that
+//     sequence by bucket (so each bucket's run is in rank order), run starts
+//     and lengths by scans, and the list position of each record as
+//     (records in runs whose head ranks later) + (later records of its run);
+//   * output slots and value offsets: exclusive scans of the kept flags and
+//     popcounts in list order.
+// ---------------------------------------------------------------------------
+struct BigShared {
+    int32_t hist[256];                     // digit bases of the pass
+    int32_t tile_tot[256];                 // digit counts of the tile
+    int32_t wcnt[kBigThreads / 32][256];   // per-warp digit counts, then prefixes
+    int32_t warp_tot[kBigThreads / 32];
+    int32_t carry;
+};
+
+struct BigRecs {
+    const uint64_t* code;
+    const int64_t* bcol;
+    int32_t* ins;
+    int32_t* tau;
+    uint32_t* bkt;
+    int32_t* g;
+    int32_t* pos;
+    int32_t* pops;
+    int32_t* k0;
+    int32_t* v0;
+    int32_t* k1;
+    int32_t* v1;
+};
+
+// In-place block-wide scan of a[0, n) (1024 threads, tiles of 1024): an
+// exclusive or inclusive sum, or (MAX) an inclusive max.
+template <bool MAX>
+__device__ void big_scan(BigShared& sh, int32_t* a, int n, bool inclusive) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int32_t ident = MAX ? INT32_MIN : 0;
+    auto op = [](int32_t x, int32_t y) { return MAX ? (x > y ? x : y) : x + y; };
+    if (t == 0) sh.carry = ident;
+    __syncthreads();
+    for (int base = 0; base < n; base += kBigThreads) {
+        const int i = base + t;
+        const int32_t x = i < n ? a[i] : ident;
+        int32_t v = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t u = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v = op(u, v);
+        }
+        if (lane == 31) sh.warp_tot[warp] = v;
+        __syncthreads();
+        if (warp == 0) {
+            int32_t wv = sh.warp_tot[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int32_t u = __shfl_up_sync(0xffffffffu, wv, o);
+                if (lane >= o) wv = op(u, wv);
+            }
+            sh.warp_tot[lane] = wv;   // inclusive over the warps
+        }
+        __syncthreads();
+        const int32_t c = sh.carry;
+        const int32_t incl = op(c, warp > 0 ? op(sh.warp_tot[warp - 1], v) : v);
+        if (i < n) a[i] = (inclusive || MAX) ? incl : incl - x;
+        __syncthreads();
+        if (t == 0) sh.carry = op(c, sh.warp_tot[kBigThreads / 32 - 1]);
+        __syncthreads();
+    }
+}
+
+// Stable LSD radix sort (8-bit digits) of (key, val) pairs, n elements, keys
+// read as unsigned and below 2^bits.  Ping-pongs between (k, v) and (kt, vt)
+// for an even number of passes, so the result ends in (k, v).
+__device__ void big_sort(BigShared& sh, int32_t* k, int32_t* v, int32_t* kt, int32_t* vt, int n, int bits) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    int passes = (bits + 7) / 8;
+    if (passes < 2) passes = 2;
+    if (passes & 1) ++passes;
+    for (int pass = 0; pass < passes; ++pass) {
+        const int shift = 8 * pass;
+        const int32_t* ks = (pass & 1) ? kt : k;
+        const int32_t* vs = (pass & 1) ? vt : v;
+        int32_t* kd = (pass & 1) ? k : kt;
+        int32_t* vd = (pass & 1) ? v : vt;
+        if (t < 256) sh.hist[t] = 0;
+        __syncthreads();
+        for (int i = t; i < n; i += kBigThreads) atomicAdd(&sh.hist[((uint32_t)ks[i] >> shift) & 255u], 1);
+        __syncthreads();
+        if (warp == 0) {   // exclusive scan of the histogram: digit bases
+            int32_t run = 0;
+            for (int d0 = 0; d0 < 256; d0 += 32) {
+                const int32_t x = sh.hist[d0 + lane];
+                int32_t incl = x;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += u;
+                }
+                sh.hist[d0 + lane] = run + incl - x;
+                run += __shfl_sync(0xffffffffu, incl, 31);
+            }
+        }
+        __syncthreads();
+        for (int base = 0; base < n; base += kBigThreads) {   // tiles in order: stable
+            const int i = base + t;
+            const bool ok = i < n;
+            const int32_t key = ok ? ks[i] : 0;
+            const int32_t val = ok ? vs[i] : 0;
+            const int d = ok ? (int)(((uint32_t)key >> shift) & 255u) : 256;
+            for (int q = lane; q < 256; q += 32) sh.wcnt[warp][q] = 0;
+            __syncwarp();
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            const int lrank = __popc(peers & ((1u << lane) - 1u));
+            if (ok && lrank == 0) sh.wcnt[warp][d] = __popc(peers);
+            __syncthreads();
+            if (t < 256) {   // per digit: exclusive prefix over the warps
+                int32_t run = 0;
+                for (int w2 = 0; w2 < kBigThreads / 32; ++w2) {
+                    const int32_t c = sh.wcnt[w2][t];
+                    sh.wcnt[w2][t] = run;
+                    run += c;
+                }
+                sh.tile_tot[t] = run;
+            }
+            __syncthreads();
+            if (ok) {
+                const int dst = sh.hist[d] + sh.wcnt[warp][d] + lrank;
+                kd[dst] = key;
+                vd[dst] = val;
+            }
+            __syncthreads();
+            if (t < 256) sh.hist[t] += sh.tile_tot[t];
+            __syncthreads();
+        }
+    }
+}
+
+// list_order for a big stripe: list positions (pos) of the records with
+// insertion rank < present under `buckets`, given their ranks tau (a
+// permutation of [0, present) over those records).
+__device__ void list_order_big(BigShared& sh, int64_t s, int64_t ncb, bool key32, uint64_t buckets, int m,
+                               int present, const BigRecs& r) {
+    const int t = threadIdx.x;
+    for (int e = t; e < m; e += kBigThreads) {
+        if (r.ins[e] >= present) continue;
+        const uint32_t b = key_bucket(s * ncb + r.bcol[e], key32, buckets);
+        r.bkt[e] = b;
+        r.v0[r.tau[e]] = e;   // records in rank order
+    }
+    __syncthreads();
+    for (int i = t; i < present; i += kBigThreads) r.k0[i] = (int32_t)r.bkt[r.v0[i]];
+    __syncthreads();
+    const int bits = buckets > 1 ? 64 - __clzll((long long)(buckets - 1)) : 1;
+    big_sort(sh, r.k0, r.v0, r.k1, r.v1, present, bits);   // bucket runs, each in rank order
+    for (int i = t; i < present; i += kBigThreads) r.k1[i] = (i == 0 || r.k0[i] != r.k0[i - 1]) ? i : -1;
+    __syncthreads();
+    big_scan<true>(sh, r.k1, present, true);   // k1[i] = first sorted index of i's run
+    for (int i = t; i < present; i += kBigThreads) {
+        const bool last = (i + 1 == present) || (r.k0[i + 1] != r.k0[i]);
+        if (last) r.v1[r.k1[i]] = i - r.k1[i] + 1;   // run length, at the run start
+    }
+    __syncthreads();
+    // head rank of each record's run, and its later run-mates
+    for (int i = t; i < present; i += kBigThreads) {
+        const int e = r.v0[i];
+        const int st = r.k1[i];
+        r.g[e] = r.tau[r.v0[st]];
+        r.pos[e] = r.v1[st] - 1 - (i - st);
+    }
+    __syncthreads();
+    // run sizes indexed by head rank, inclusive prefix: records in runs whose
+    // head is at most h; the runs with later heads come first in the list
+    for (int h = t; h < present; h += kBigThreads) r.k0[h] = 0;
+    __syncthreads();
+    for (int i = t; i < present; i += kBigThreads)
+        if (r.k1[i] == i) r.k0[r.tau[r.v0[i]]] = r.v1[i];
+    __syncthreads();
+    big_scan<false>(sh, r.k0, present, true);
+    const int32_t total = present;
+    for (int e = t; e < m; e += kBigThreads)
+        if (r.ins[e] < present) r.pos[e] += total - r.k0[r.g[e]];
+    __syncthreads();
+}
+
+// order_stripe for a big stripe (one 1024-thread CTA; see the section
+// comment above).  Same outputs as order_stripe.
+template <typename I>
+__device__ void order_stripe_big(BigShared& sh, int64_t s, int m, int br, int bc, int min_nnz, int64_t ncb,
+                                 bool key32, int nchain, const int64_t* chain, int64_t prefmax, int64_t kept_base,
+                                 int64_t packed_base, const BigRecs& r, uint64_t* out_codes, I* out_coords,
+                                 I* out_offsets) {
+    const int t = threadIdx.x;
+    for (int e = t; e < m; e += kBigThreads) {
+        r.pops[e] = __popcll(r.code[e]);
+        r.k0[e] = r.ins[e];
+        r.v0[e] = e;
+    }
+    __syncthreads();
+    big_sort(sh, r.k0, r.v0, r.k1, r.v1, m, 31);   // by first CSR position
+    for (int i = t; i < m; i += kBigThreads) r.ins[r.v0[i]] = i;   // insertion rank
+    __syncthreads();
+    for (int e = t; e < m; e += kBigThreads) r.tau[e] = r.ins[e];
+    __syncthreads();
+    int J = 0;
+    while (J + 1 < nchain && chain[2 * (J + 1)] <= prefmax) ++J;
+    while (J + 1 < nchain && chain[2 * (J + 1)] <= m) {
+        const int present = (int)(chain[2 * (J + 1)] - 1);
+        list_order_big(sh, s, ncb, key32, (uint64_t)chain[2 * J + 1], m, present, r);
+        for (int e = t; e < m; e += kBigThreads)
+            if (r.ins[e] < present) r.tau[e] = r.pos[e];
+        __syncthreads();
+        ++J;
+    }
+    list_order_big(sh, s, ncb, key32, (uint64_t)chain[2 * J + 1], m, m, r);
+    // kept flags and popcounts in list order; exclusive scans give slots and
+    // value offsets
+    for (int e = t; e < m; e += kBigThreads) {
+        const bool kept = r.pops[e] >= min_nnz;
+        r.k0[r.pos[e]] = kept ? 1 : 0;
+        r.v0[r.pos[e]] = kept ? r.pops[e] : 0;
+    }
+    __syncthreads();
+    big_scan<false>(sh, r.k0, m, false);
+    big_scan<false>(sh, r.v0, m, false);
+    for (int e = t; e < m; e += kBigThreads) {
+        int slot = -1, doff = 0;
+        if (r.pops[e] >= min_nnz) {
+            slot = r.k0[r.pos[e]];
+            doff = r.v0[r.pos[e]];
+            const int64_t ob = kept_base + slot;
+            out_codes[ob] = r.code[e];
+            out_coords[2 * ob] = (I)(s * br);
+            out_coords[2 * ob + 1] = (I)(r.bcol[e] * bc);
+            out_offsets[ob] = (I)(packed_base + doff);
+        }
+        r.tau[e] = slot;
+        r.g[e] = doff;
+    }
+    __syncthreads();
 }
 
 // Emit order and outputs of one stripe's m recorded blocks (team-parallel).
@@ -441,9 +691,7 @@ build_fill_big_kernel(const I* indptr, const I* indices, const S* values, int64_
                       int br, int bc, int min_nnz, int64_t nstripes, int64_t ncb, bool key32, int nchain,
                       BuildWs w, uint64_t* out_codes, I* out_coords, I* out_offsets, S* out_data,
                       I* out_rem_col, S* out_rem_val) {
-    __shared__ int32_t sh_ins[kBigStage], sh_tau[kBigStage], sh_g[kBigStage], sh_pos[kBigStage];
-    __shared__ int32_t sh_pops[kBigStage];
-    __shared__ uint32_t sh_bkt[kBigStage];
+    __shared__ BigShared sh;
     for (int64_t s = blockIdx.x; s < nstripes; s += gridDim.x) {
         const int64_t rbase = w.stripe_m[s];
         const int m = (int)(w.stripe_m[s + 1] - rbase);
@@ -452,27 +700,11 @@ build_fill_big_kernel(const I* indptr, const I* indices, const S* values, int64_
             record_blocks<I>(indptr, indices, s, rows, cols, nnz, br, bc, w.rec_code + rbase, w.rec_bcol + rbase,
                              w.rec_ins + rbase);
         __syncthreads();
-        const bool staged = m <= kBigStage;
-        int32_t* ins = staged ? sh_ins : w.rec_ins + rbase;
-        int32_t* tau = staged ? sh_tau : w.rec_tau + rbase;
-        int32_t* g = staged ? sh_g : w.rec_g + rbase;
-        int32_t* pos = staged ? sh_pos : w.rec_pos + rbase;
-        int32_t* pops = staged ? sh_pops : w.rec_pops + rbase;
-        uint32_t* bkt = staged ? sh_bkt : w.rec_bkt + rbase;
-        if (staged)
-            for (int e = threadIdx.x; e < m; e += kBigThreads) ins[e] = w.rec_ins[rbase + e];
-        __syncthreads();
-        order_stripe<kBigThreads, I>(s, m, br, bc, min_nnz, ncb, key32, nchain, w.chain, w.stripe_prefmax[s],
-                                     w.stripe_kept[s], w.stripe_packed[s], w.rec_code + rbase, w.rec_bcol + rbase,
-                                     ins, tau, bkt, g, pos, pops, out_codes, out_coords, out_offsets);
-        // slot -> tau, value offset -> g; move_values reads them from global
-        if (staged) {
-            for (int e = threadIdx.x; e < m; e += kBigThreads) {
-                w.rec_tau[rbase + e] = tau[e];
-                w.rec_g[rbase + e] = g[e];
-            }
-        }
-        __syncthreads();
+        BigRecs r{w.rec_code + rbase, w.rec_bcol + rbase, w.rec_ins + rbase, w.rec_tau + rbase,
+                  w.rec_bkt + rbase, w.rec_g + rbase, w.rec_pos + rbase, w.rec_pops + rbase,
+                  w.rec_k0 + rbase, w.rec_v0 + rbase, w.rec_k1 + rbase, w.rec_v1 + rbase};
+        order_stripe_big<I>(sh, s, m, br, bc, min_nnz, ncb, key32, nchain, w.chain, w.stripe_prefmax[s],
+                            w.stripe_kept[s], w.stripe_packed[s], r, out_codes, out_coords, out_offsets);
         if (threadIdx.x < 32)
             move_values<I, S>(indptr, indices, values, s, rows, cols, nnz, br, bc, w.rec_tau + rbase,
                               w.rec_g + rbase, w.stripe_packed[s], w.row_rem, out_data, out_rem_col, out_rem_val);

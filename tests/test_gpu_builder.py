@@ -101,3 +101,21 @@ def test_noncanonical_input_is_canonicalized(device):
     want = oracle.csr_to_pbr(C.indptr, C.indices, C.data, 4, 4, 2, 2, 2)
     _, got = _gpu(A, 2, 2, 2)
     assert_pbr_equal(got, want, "canonicalized")
+
+
+def test_builder_hub_stripes_vs_oracle(device):
+    """Clustered R-MAT graph whose hub rows put hundreds to thousands of
+    distinct blocks into one stripe (the one-CTA ordering path, with rehashes
+    inside the stripe), several block shapes."""
+    from page_rank_gb300 import synth
+    g = synth.cluster_rmat_graph(log2n=15, cluster=64, mean_degree=16, p_intra=0.7, seed=4)
+    A = g.A
+    n = A.shape[0]
+    rows = np.repeat(np.arange(n), np.diff(A.indptr))
+    key = (rows // 8).astype(np.int64) * (n // 8 + 1) + A.indices // 8
+    distinct = np.bincount(np.unique(key) // (n // 8 + 1))
+    assert distinct.max() > 1000 and (distinct > 64).sum() > 300
+    for br, mn in ((8, 8), (4, 2), (2, 1)):
+        want = oracle.csr_to_pbr(A.indptr, A.indices, A.data, n, A.shape[1], br, br, mn)
+        _, got = _gpu(A, br, br, mn)
+        assert_pbr_equal(got, want, f"hub b={br} min={mn}")
