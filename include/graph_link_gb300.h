@@ -274,6 +274,10 @@ typedef struct gl_ppr_step_params {
     double*         dangling_hist;    /* device [max_iterations + 1][K]      */
     const uint32_t* dangling_bitmap;  /* device, ceil(rows/32) words, or NULL */
     int32_t         dangling_target;  /* GL_DANGLING_TO_TELEPORT / _UNIFORM  */
+    const double*   column_alpha;     /* device [K]: alpha of each column, or
+                                         NULL: alpha for every column         */
+    const double*   column_tol;       /* device [K]: STOP_PER_COLUMN threshold
+                                         of each column, or NULL: tol         */
 } gl_ppr_step_params;
 
 int gl_ppr_step(const gl_pbr_matrix* A, const gl_teleport* tp,

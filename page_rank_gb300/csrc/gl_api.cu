@@ -398,7 +398,9 @@ extern "C" int gl_ppr_step(const gl_pbr_matrix* A, const gl_teleport* tp, const 
     (a).res_hist = p->residual_hist;                       \
     (a).dang_hist = p->dangling_hist;                      \
     (a).dbitmap = p->dangling_bitmap;                      \
-    (a).dang_uniform = p->dangling_target == GL_DANGLING_UNIFORM
+    (a).dang_uniform = p->dangling_target == GL_DANGLING_UNIFORM; \
+    (a).col_alpha = p->column_alpha;                       \
+    (a).col_tol = p->column_tol
     if (A->value_type == GL_F32) {
         StripeArgs<float> a = make_args<float>(A);
         GL_FILL_PPR(a);

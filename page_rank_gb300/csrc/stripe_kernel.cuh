@@ -116,6 +116,8 @@ struct StripeArgs {
     double* dang_hist;
     const uint32_t* dbitmap;
     int32_t dang_uniform;
+    const double* col_alpha;       // [K] or nullptr: alpha for every column
+    const double* col_tol;         // [K] or nullptr: tol for every column
 };
 
 template <typename S, int V>
@@ -527,12 +529,12 @@ stripe_kernel(const StripeArgs<S> a) {
         }
     }
 
-    const S alpha = static_cast<S>(a.alpha);
     int64_t cur_bt = -1;
     int cur_col = 0;
     bool cur_ok = false;
     S scale[V];
     S unif[V];
+    S alph[V];
     bool frozen[V];
     float res_acc[V];
     float dang_acc[V];
@@ -540,6 +542,7 @@ stripe_kernel(const StripeArgs<S> a) {
     for (int j = 0; j < V; ++j) {
         scale[j] = S(0);
         unif[j] = S(0);
+        alph[j] = S(0);
         frozen[j] = false;
         res_acc[j] = 0.f;
         dang_acc[j] = 0.f;
@@ -628,17 +631,20 @@ stripe_kernel(const StripeArgs<S> a) {
 #pragma unroll
                     for (int j = 0; j < V; ++j) {
                         const int col = col_base + j;
-                        double sc = 1.0 - a.alpha;
+                        const double al = a.col_alpha != nullptr ? a.col_alpha[col] : a.alpha;
+                        const double tl = a.col_tol != nullptr ? a.col_tol[col] : a.tol;
+                        double sc = 1.0 - al;
                         double un = 0.0;
                         if (a.dbitmap != nullptr) {
-                            const double d = a.alpha * a.dang_hist[(int64_t)t * a.K + col];
+                            const double d = al * a.dang_hist[(int64_t)t * a.K + col];
                             if (a.dang_uniform) un = d / (double)a.rows;
                             else sc += d;
                         }
                         scale[j] = static_cast<S>(sc);
                         unif[j] = static_cast<S>(un);
+                        alph[j] = static_cast<S>(al);
                         frozen[j] = (a.stop_mode == GL_PPR_STOP_PER_COLUMN && t > 0 &&
-                                     a.res_hist[(int64_t)(t - 1) * a.K + col] < a.tol);
+                                     a.res_hist[(int64_t)(t - 1) * a.K + col] < tl);
                     }
                 }
             }
@@ -797,7 +803,7 @@ stripe_kernel(const StripeArgs<S> a) {
                 for (int r = 0; r < BR; ++r) {
                     Pack<S, V> o = load_pack<S, V>(tw + r * T);
 #pragma unroll
-                    for (int j = 0; j < V; ++j) o.v[j] = fma(alpha, o.v[j], unif[j]);
+                    for (int j = 0; j < V; ++j) o.v[j] = fma(alph[j], o.v[j], unif[j]);
                     store_pack<S, V>(tw + r * T, o);
                 }
                 const int32_t e0 = a.tp_ptr[s], e1 = a.tp_ptr[s + 1];

@@ -143,7 +143,7 @@ class PprStepParams(_c.Structure):
     _fields_ = [("alpha", _c.c_double), ("tol", _c.c_double), ("stop_mode", _i32),
                 ("max_iterations", _i32), ("step_in_chunk", _i32), ("chunk_base", _vp),
                 ("residual_hist", _vp), ("dangling_hist", _vp), ("dangling_bitmap", _vp),
-                ("dangling_target", _i32)]
+                ("dangling_target", _i32), ("column_alpha", _vp), ("column_tol", _vp)]
 
 
 # name -> (restype, argtypes)

@@ -107,13 +107,31 @@ class PprRun:
         self.block_rows, self.block_cols = block_rows, block_cols
         self.tp = teleport
         self.K = teleport.num_columns
+        dev = meta["data"].device
+        # alpha / tol: one value for all columns, or one per column (a column
+        # of the batch then runs exactly as it would alone with its own pair)
+        self.col_alpha = self.col_tol = None
+        if np.ndim(alpha):
+            a = np.asarray(alpha, dtype=np.float64)
+            if a.shape != (self.K,):
+                raise ValueError("alpha must be a scalar or have one entry per column")
+            self.col_alpha = torch.from_numpy(a).to(dev)
+            alpha = float(a.max()) if a.size else 0.85
+        if np.ndim(tol):
+            tv = np.asarray(tol, dtype=np.float64)
+            if tv.shape != (self.K,):
+                raise ValueError("tol must be a scalar or have one entry per column")
+            self.col_tol = torch.from_numpy(tv).to(dev)
+            self.tol_host = tv
+            tol = float(tv.min()) if tv.size else 0.0
+        else:
+            self.tol_host = np.full(self.K, float(tol))
         self.alpha = float(alpha)
         self.max_iterations = int(max_iterations)
         self.tol = float(tol)
         self.stop_mode = stop_mode
         self.dangling_bits = dangling_bits
         self.dangling_target = dangling_target
-        dev = meta["data"].device
         dtype = meta["data"].dtype
         self.device = dev
         self.bufs = [torch.empty((rows, self.K), dtype=dtype, device=dev),
@@ -161,6 +179,8 @@ class PprRun:
             p.dangling_hist = self.dang_hist.data_ptr()
             p.dangling_bitmap = _ptr(self.dangling_bits)
             p.dangling_target = self.dangling_target
+            p.column_alpha = _ptr(self.col_alpha)
+            p.column_tol = _ptr(self.col_tol)
             self._params.append(p)
         return self._params[i]
 
@@ -206,7 +226,7 @@ class PprRun:
             for t in range(n):
                 row = res[t]
                 history.append(float(row.max()) if self.K else 0.0)
-                newly = (col_iter < 0) & (row < self.tol)
+                newly = (col_iter < 0) & (row < self.tol_host)
                 col_iter[newly] = done + t + 1
                 if self.stop_mode == native.GL_PPR_STOP_ALL:
                     if self.K and row.max() < self.tol:

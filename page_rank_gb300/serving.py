@@ -2,8 +2,10 @@
 
 Graphs stay resident in HBM as PBR matrices (one :class:`PPREngine` each).
 Requests (graph, seed set, alpha, tolerance) arrive at any time; the
-scheduler keeps one *slot batch* per (graph, alpha) group: the columns of one
-fused power iteration.  Between chunks of iterations it
+scheduler keeps one *slot batch* per graph: the columns of one fused power
+iteration, each column with its own alpha and certified threshold (one pass
+over the matrix serves every request of the graph).  Between chunks of
+iterations it
 
 * retires columns whose update fell below their (certified) tolerance and
   hands their vectors to the waiting callers,
@@ -58,12 +60,11 @@ class Request:
 
 
 class _Group:
-    """The slot batch of one (graph, alpha) pair."""
+    """The slot batch of one graph."""
 
-    def __init__(self, server: "PPRServer", graph: str, alpha: float):
+    def __init__(self, server: "PPRServer", graph: str):
         self.server = server
         self.graph = graph
-        self.alpha = alpha
         self.eng: PPREngine = server.engines[graph]
         self.stream = torch.cuda.Stream(server.device)
         self.reqs: list[Request] = []          # live columns, in column order
@@ -85,17 +86,18 @@ class _Group:
             sets = [r.seeds for r in reqs]
             ptr, rows, w = self.eng.teleport(sets)
             tp = teleport_from_seed_sets(ptr, rows, self.eng.n, self.eng.block_size, w)
-            thr = min(certified_tolerance(r.tol, self.alpha) for r in reqs)
+            alphas = np.array([r.alpha for r in reqs], dtype=np.float64)
+            thr = np.array([certified_tolerance(r.tol, r.alpha) for r in reqs], dtype=np.float64)
             max_it = max(r.max_iterations for r in reqs)
             run = PprRun(self.eng.meta, self.eng.n, self.eng.n, self.eng.block_size, self.eng.block_size, tp,
-                         self.alpha, max_it, thr, native.GL_PPR_STOP_PER_COLUMN, self.eng.dbits)
+                         alphas, max_it, thr, native.GL_PPR_STOP_PER_COLUMN, self.eng.dbits)
             if self.joining:
                 x0 = torch.empty((self.eng.n, len(reqs)), dtype=torch.float32, device=dev)
                 if x_keep is not None and self.reqs:
                     x0[:, : len(self.reqs)] = x_keep
                 j0 = len(self.reqs)
-                x_new = self.server.start_vectors(self.graph, [r.seeds for r in self.joining], self.alpha,
-                                                  self.stream)
+                x_new = self.server.start_vectors(self.graph, [r.seeds for r in self.joining],
+                                                  np.array([r.alpha for r in self.joining]), self.stream)
                 x0[:, j0:] = x_new
             else:
                 x0 = x_keep
@@ -124,7 +126,7 @@ class _Group:
         self.pending = False
         finished = []
         for c, r in enumerate(self.reqs):
-            thr_c = certified_tolerance(r.tol, self.alpha)
+            thr_c = certified_tolerance(r.tol, r.alpha)
             col = res[:, c] if res.size else np.zeros(0)
             hit = np.nonzero(col < thr_c)[0]
             if hit.size:
@@ -207,7 +209,7 @@ class PPRServer:
             tot += (len(g.reqs) + len(g.joining)) * self.column_bytes(g.graph)
         return tot
 
-    def start_vectors(self, graph: str, seed_sets, alpha: float, stream) -> torch.Tensor:
+    def start_vectors(self, graph: str, seed_sets, alpha, stream) -> torch.Tensor:
         """Initial columns for newly admitted requests: learned warm start where
         available (with its cold-start fallback), else the teleport vector."""
         eng = self.engines[graph]
@@ -246,7 +248,7 @@ class PPRServer:
         still = collections.deque()
         while self.waiting:
             r = self.waiting.popleft()
-            key = (r.graph, r.alpha)
+            key = r.graph
             g = self.groups.get(key)
             live = (len(g.reqs) + len(g.joining)) if g else 0
             need = self.column_bytes(r.graph)
@@ -255,7 +257,7 @@ class PPRServer:
                 self.admission_waits += 1
                 continue
             if g is None:
-                g = self.groups[key] = _Group(self, r.graph, r.alpha)
+                g = self.groups[key] = _Group(self, r.graph)
             g.joining.append(r)
             r.t_admit = time.perf_counter()
             budget_left -= need

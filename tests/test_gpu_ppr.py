@@ -98,3 +98,40 @@ def test_ppr_float64_matrix(device):
     V = oppr.teleport_matrix(50, [[7]])
     X64 = oppr.direct_solve_fp64(A, V, 0.85)
     assert np.abs(X.cpu().numpy() - X64).sum() < 1e-8
+
+
+@pytest.mark.parametrize("K", [4, 40])
+def test_ppr_per_column_alpha_matches_scalar_runs(K, device):
+    """Columns with their own alpha / certified threshold in one fused run
+    give bit for bit the vectors of runs where every column has that alpha,
+    and each is within L1 1e-6 of its FP64 fixed point."""
+    from page_rank_gb300 import native, synth
+    from page_rank_gb300.engine import PPREngine, certified_tolerance
+    from page_rank_gb300.ppr import PprRun, teleport_from_seed_sets
+    g = synth.cluster_zipf_graph(log2n=12, mean_degree=8.0, seed=3)
+    n = g.n
+    eng = PPREngine(g.A, block_size=4, min_nnz_per_block=4, device=device, dangling=g.dangling)
+    rng = np.random.default_rng(7)
+    sets = [rng.choice(n, size=int(rng.integers(1, 6)), replace=False) for _ in range(K)]
+    alphas = np.array([(0.8, 0.85, 0.9)[k % 3] for k in range(K)])
+    thr = np.array([certified_tolerance(1e-6, a) for a in alphas])
+
+    def run(alpha, tol):
+        ptr, rows, w = eng.teleport(sets)
+        tp = teleport_from_seed_sets(ptr, rows, n, 4, w)
+        r = PprRun(eng.meta, n, n, 4, 4, tp, alpha, 1000, tol, native.GL_PPR_STOP_PER_COLUMN, eng.dbits)
+        return r.run(chunk=8)
+
+    mixed = run(alphas, thr)
+    assert mixed.converged
+    for a in (0.8, 0.85, 0.9):
+        single = run(a, certified_tolerance(1e-6, a))
+        cols = np.nonzero(alphas == a)[0]
+        assert torch.equal(mixed.X[:, cols], single.X[:, cols])
+    V = oppr.teleport_matrix(n, sets)
+    X = mixed.X.cpu().numpy().astype(np.float64)
+    for a in (0.8, 0.85, 0.9):
+        cols = np.nonzero(alphas == a)[0]
+        want, _, ok, _ = oppr.power_iteration_fp64(g.A, V[:, cols], a, 5000, 1e-14, g.dangling)
+        assert ok
+        assert np.abs(X[:, cols] - want).sum(axis=0).max() <= 1e-6
