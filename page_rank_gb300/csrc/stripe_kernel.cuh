@@ -481,10 +481,37 @@ struct StripeSmem {
 #ifndef GL_STRIPE_MIN_CTAS
 #define GL_STRIPE_MIN_CTAS 4
 #endif
+#ifndef GL_PPR_MIN_CTAS
+#define GL_PPR_MIN_CTAS 3
+#endif
 template <typename S, int V, bool PPR>
 struct MinBlocks {
-    static constexpr int n = (PPR && sizeof(S) * V >= 16) ? 3 : GL_STRIPE_MIN_CTAS;
+    static constexpr int n = (PPR && sizeof(S) * V >= 16) ? GL_PPR_MIN_CTAS : GL_STRIPE_MIN_CTAS;
 };
+
+// One column's terms of power-iteration step t: the alpha that scales A x,
+// the teleport scale (1 - alpha, plus the dangling mass when it goes to the
+// teleport vector), the uniform dangling share, and whether the column has
+// converged (STOP_PER_COLUMN).
+struct ColumnTerms {
+    double alpha, scale, uniform;
+    bool frozen;
+};
+template <typename S>
+__device__ __forceinline__ ColumnTerms column_terms(const StripeArgs<S>& a, int t, int col) {
+    ColumnTerms c;
+    c.alpha = a.col_alpha != nullptr ? a.col_alpha[col] : a.alpha;
+    const double tl = a.col_tol != nullptr ? a.col_tol[col] : a.tol;
+    c.scale = 1.0 - c.alpha;
+    c.uniform = 0.0;
+    if (a.dbitmap != nullptr) {
+        const double d = c.alpha * a.dang_hist[(int64_t)t * a.K + col];
+        if (a.dang_uniform) c.uniform = d / (double)a.rows;
+        else c.scale += d;
+    }
+    c.frozen = a.stop_mode == GL_PPR_STOP_PER_COLUMN && t > 0 && a.res_hist[(int64_t)(t - 1) * a.K + col] < tl;
+    return c;
+}
 
 template <typename S, int BR, int BC, int V, int C, bool PPR>
 __global__ void __launch_bounds__(kStripeThreads, MinBlocks<S, V, PPR>::n)
@@ -532,18 +559,10 @@ stripe_kernel(const StripeArgs<S> a) {
     int64_t cur_bt = -1;
     int cur_col = 0;
     bool cur_ok = false;
-    S scale[V];
-    S unif[V];
-    S alph[V];
-    bool frozen[V];
     float res_acc[V];
     float dang_acc[V];
 #pragma unroll
     for (int j = 0; j < V; ++j) {
-        scale[j] = S(0);
-        unif[j] = S(0);
-        alph[j] = S(0);
-        frozen[j] = false;
         res_acc[j] = 0.f;
         dang_acc[j] = 0.f;
     }
@@ -627,26 +646,6 @@ stripe_kernel(const StripeArgs<S> a) {
                 cur_bt = bt;
                 cur_col = col_base;
                 cur_ok = lane_ok && p_lane == 0;
-                if (lane_ok) {
-#pragma unroll
-                    for (int j = 0; j < V; ++j) {
-                        const int col = col_base + j;
-                        const double al = a.col_alpha != nullptr ? a.col_alpha[col] : a.alpha;
-                        const double tl = a.col_tol != nullptr ? a.col_tol[col] : a.tol;
-                        double sc = 1.0 - al;
-                        double un = 0.0;
-                        if (a.dbitmap != nullptr) {
-                            const double d = al * a.dang_hist[(int64_t)t * a.K + col];
-                            if (a.dang_uniform) un = d / (double)a.rows;
-                            else sc += d;
-                        }
-                        scale[j] = static_cast<S>(sc);
-                        unif[j] = static_cast<S>(un);
-                        alph[j] = static_cast<S>(al);
-                        frozen[j] = (a.stop_mode == GL_PPR_STOP_PER_COLUMN && t > 0 &&
-                                     a.res_hist[(int64_t)(t - 1) * a.K + col] < tl);
-                    }
-                }
             }
         }
 
@@ -798,6 +797,17 @@ stripe_kernel(const StripeArgs<S> a) {
                     if (row < a.rows) store_pack<S, V>(Yb + row * a.K, load_pack<S, V>(trow + r * T));
                 }
             } else {
+                // this step's per-column terms (computed here, not kept in
+                // registers across the accumulation)
+                S alph[V], unif[V];
+                bool frozen[V];
+#pragma unroll
+                for (int j = 0; j < V; ++j) {
+                    const ColumnTerms ct = column_terms(a, t, col_base + j);
+                    alph[j] = static_cast<S>(ct.alpha);
+                    unif[j] = static_cast<S>(ct.uniform);
+                    frozen[j] = ct.frozen;
+                }
                 S* tw = otile + c_lane * V;
 #pragma unroll 2
                 for (int r = 0; r < BR; ++r) {
@@ -811,10 +821,7 @@ stripe_kernel(const StripeArgs<S> a) {
                     const int rr = a.tp_row[e] - (int)(s * BR);
                     const int cc = a.tp_col[e] - col_base;
                     if (cc >= 0 && cc < V) {
-                        S sc = scale[0];
-#pragma unroll
-                        for (int j = 1; j < V; ++j)
-                            if (j == cc) sc = scale[j];
+                        const S sc = static_cast<S>(column_terms(a, t, col_base + cc).scale);
                         tw[rr * T + cc] = fma(static_cast<S>(a.tp_w[e]), sc, tw[rr * T + cc]);
                     }
                 }

@@ -52,7 +52,7 @@ def ppr_batched(device, log2n: int = 22, K: int = 256, plain_sample: int = 16, t
     eng = PPREngine(g.A, block_size=bs, min_nnz_per_block=mn, device=device, dangling=g.dangling,
                     column_tile=tile)
     # batched: all K seed sets as columns, retirement + CUDA graphs
-    eng.solve(sets[:8], alpha=0.85, tol=1e-6)                       # warm-up (captures, caches)
+    eng.solve(sets, alpha=0.85, tol=1e-6)      # warm-up: every launch shape and workspace once
     torch.cuda.synchronize(device)
     rb = eng.solve(sets, alpha=0.85, tol=1e-6, retire=True, use_graphs=True)
     batched_qps = K / rb.seconds
