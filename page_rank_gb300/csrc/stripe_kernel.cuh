@@ -8,18 +8,18 @@
 // the warp's shared memory and is written to Y once — no atomics on the
 // output, no pre-zeroed output, no second stream.
 //
-//   * P <= 2 (32 or more columns): per chunk of 32 blocks the lanes decode
-//     one block each (metadata in registers, one packed warp scan of the
-//     per-row bit counts) into row-sorted (column, value) lists in shared
-//     memory, followed by each row's CSR-remainder entries; the warp then
-//     walks one row at a time, issuing GL_GATHER_DEPTH X-row gathers before
-//     their FMAs into one V-wide accumulator, and adds the row to the tile.
-//     Values are packed in row-major bit order, so a block's entries of one
-//     row are a contiguous run.
-//   * P > 2 (fewer than 32 columns): the nonzero lanes stride the blocks
-//     (staging the X rows of each block's active columns in shared memory)
-//     and the remainder entries, with block_rows x V accumulators in
-//     registers folded by shuffles into the tile.
+//   * decode: per chunk of 32 blocks the lanes take one block each
+//     (metadata in registers, one packed warp scan of the per-row bit
+//     counts) and write row-sorted (column, value) lists in shared memory,
+//     followed by each row's CSR-remainder entries.  Values are packed in
+//     row-major bit order, so a block's entries of one row are a contiguous
+//     run.
+//   * P <= 2 (32 or more columns): the warp walks one row at a time,
+//     issuing GL_GATHER_DEPTH X-row gathers before their FMAs into one
+//     V-wide accumulator, and adds the row to the tile.
+//   * P > 2 (fewer than 32 columns, one column per lane): P consecutive
+//     entries per round, one per group of C column lanes, summed per row by
+//     a segmented warp scan.
 //
 // Load balance: stripes whose stored entries exceed 2 x piece_work (R-MAT
 // hub rows reach tens of thousands) are cut into pieces of piece_work
@@ -44,9 +44,7 @@
 namespace gl {
 
 constexpr int kStripeThreads = 256;
-#ifndef GL_STATIC_PERCENT
-#define GL_STATIC_PERCENT 0
-#endif
+
 constexpr int kStripeWarps = kStripeThreads / 32;
 
 // Workspace of one SpMM / power-iteration launch (caller-provided or the
@@ -96,14 +94,11 @@ struct StripeArgs {
     const int32_t* piece_heavy;    // [num_pieces]
     S* partial;                    // [num_pieces][batch * ntiles][BR][T]
     int32_t* counters;             // [num_heavy][batch * ntiles], zero between calls
-    // work distribution: items [0, static_items) go round-robin over the
-    // warps, the rest are drawn from sched[0] by whichever warp is free;
+    // work distribution: units are drawn one at a time from sched[0];
     // sched[1] counts retired warps.  Both are zero between calls (the last
-    // warp to retire resets them).  sched == nullptr: all items are static.
-    // (GL_STATIC_PERCENT sets the static share; drawing everything measured
-    // fastest: stripe costs vary too much for any fixed split.)
+    // warp to retire resets them).  sched == nullptr: static round-robin
+    // over the warps.
     unsigned long long* sched;
-    int64_t static_items;
     // power-iteration epilogue
     const int32_t* tp_ptr;
     const int32_t* tp_row;
@@ -186,6 +181,23 @@ __device__ __forceinline__ Entry<S> make_entry(int32_t col, S val) {
     e.val = val;
     return e;
 }
+// During decode a block entry first holds the index of its value in
+// block_data (so the value loads can be issued together afterwards).
+__device__ __forceinline__ Entry<float> make_index_entry(int32_t col, int32_t k, float) {
+    Entry<float> e;
+    e.col = col;
+    e.val = __int_as_float(k);
+    return e;
+}
+__device__ __forceinline__ Entry<double> make_index_entry(int32_t col, int32_t k, double) {
+    Entry<double> e;
+    e.col = col;
+    e.pad = k;
+    e.val = 0.0;
+    return e;
+}
+__device__ __forceinline__ int32_t entry_index(const Entry<float>& e) { return __float_as_int(e.val); }
+__device__ __forceinline__ int32_t entry_index(const Entry<double>& e) { return e.pad; }
 
 // NB gathers (entries e, e + P, ..., all issued before the first FMA) into
 // the lane's V accumulators.  Lanes past the last column gather from a
@@ -285,6 +297,62 @@ __device__ __forceinline__ void commit_row(S* tile_lane, int r, int T, S (&t)[V]
     for (int j = 0; j < V; ++j) t[j] = S(0);
 }
 
+// Walk for fewer than 32 columns (P = 32 / C > 2 entries per round, V = 1):
+// in each round the P entry lanes take P consecutive list entries and their
+// C column lanes gather one X element each; a segmented scan over the entry
+// lanes (rows are sorted) sums each row's products, and the last lane of a
+// row's segment adds the sum to the tile — deterministic, no atomics.
+// Row of entry e: the number of rows r >= 1 starting at or before e
+// (starts == nullptr: the whole list is row r_fixed).
+template <typename S, int BR, int C>
+__device__ __forceinline__ void consume_narrow(const Entry<S>* lst, int n, const int32_t* starts, int r_fixed,
+                                               S* tile, int c_lane, int p_lane, bool own_col,
+                                               const S* __restrict__ Xb, int32_t K) {
+    constexpr int P = 32 / C;
+    int32_t sv[BR];
+#pragma unroll
+    for (int r = 0; r < BR; ++r) sv[r] = starts != nullptr ? starts[r] : 0;
+    for (int base = 0; base < n; base += 2 * P) {
+        // two rounds per pass: both rounds' gathers in flight together
+        S prod[2];
+        int row[2];
+        bool valid[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int e = base + h * P + p_lane;
+            valid[h] = e < n;
+            prod[h] = S(0);
+            row[h] = r_fixed;
+            if (valid[h]) {
+                const Entry<S> en = lst[e];
+                prod[h] = en.val * Xb[(long long)en.col * K];
+                if (starts != nullptr) {
+                    int r = 0;
+#pragma unroll
+                    for (int q = 1; q < BR; ++q) r += sv[q] <= e ? 1 : 0;
+                    row[h] = r;
+                }
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            S v = prod[h];
+            const int r = row[h];
+#pragma unroll
+            for (int o = 1; o < P; o <<= 1) {
+                const S u = __shfl_up_sync(0xffffffffu, v, o * C);
+                const int ru = __shfl_up_sync(0xffffffffu, r, o * C);
+                if (p_lane >= o && ru == r) v += u;
+            }
+            const int rn = __shfl_down_sync(0xffffffffu, r, C);
+            const int e = base + h * P + p_lane;
+            const bool last = valid[h] && (p_lane == P - 1 || e + 1 >= n || rn != r);
+            if (last && own_col) tile[r * C + c_lane] += v;
+            __syncwarp();
+        }
+    }
+}
+
 // Accumulation for P <= 2 into the warp's output tile in shared memory
 // (tile[r * T + column], zeroed here, each lane its own columns).  Per chunk
 // of 32 blocks: one packed warp scan of the per-row bit counts; if the
@@ -300,7 +368,8 @@ __device__ __forceinline__ void accumulate_rows(const StripeArgs<S>& a, S* tile,
                                                 const S* __restrict__ Xb, bool lane_ok, int lane, int p_lane,
                                                 int c_lane) {
     constexpr uint32_t ROWMASK = (BC >= 32) ? 0xffffffffu : ((1u << BC) - 1u);
-    constexpr int GR = kTail * P;   // row granule
+    constexpr bool NARROW = P > 2;
+    constexpr int GR = NARROW ? 1 : kTail * P;   // row granule
     constexpr int T = (32 / P) * V;
     static_assert(kListCap % GR == 0 && kListCap >= 32 * BC + 2 * GR, "a row of one block chunk must fit the list");
     int32_t* rstart = rowinfo;
@@ -389,22 +458,58 @@ __device__ __forceinline__ void accumulate_rows(const StripeArgs<S>& a, S* tile,
                     while (rb) {
                         const int c = __ffs(rb) - 1;
                         rb &= rb - 1u;
-                        lst[pos++] = make_entry<S>(col0 + c, a.bdata[k++]);
+                        lst[pos++] = make_index_entry(col0 + c, k++, S(0));
                     }
                 }
             }
-            // remainder entries (last chunk) and padding, lane-parallel
-#pragma unroll 1
+            __syncwarp();
+            // block values and remainder entries, lane-parallel, every row's
+            // loads issued before the first store (one round trip per 32
+            // entries of the longest row, not one per entry or per row)
+            int32_t longest = 0;
+#pragma unroll
             for (int r = 0; r < BR; ++r) {
-                const int32_t sg = seg[r], bl = blen[r];
-                const int32_t rl = last ? rlen[r] : 0;
-                const int32_t rs = rstart[r];
-                for (int q = lane; q < rl; q += 32) lst[sg + bl + q] = make_entry<S>(a.rem_col[rs + q], a.rem_val[rs + q]);
-                const int32_t len = bl + rl;
+                const int32_t l = blen[r] > (last ? rlen[r] : 0) ? blen[r] : (last ? rlen[r] : 0);
+                longest = l > longest ? l : longest;
+            }
+            constexpr int RG = BR < 4 ? BR : 4;   // rows whose loads are in flight together
+            for (int j0 = 0; j0 < longest; j0 += 32) {
+                const int q = j0 + lane;
+#pragma unroll
+                for (int r0 = 0; r0 < BR; r0 += RG) {
+                    S bv[RG], rv[RG];
+                    int32_t rc[RG];
+#pragma unroll
+                    for (int h = 0; h < RG; ++h) {
+                        const int r = r0 + h;
+                        const int32_t rl = last ? rlen[r] : 0;
+                        bv[h] = q < blen[r] ? a.bdata[entry_index(lst[seg[r] + q])] : S(0);
+                        rc[h] = q < rl ? a.rem_col[rstart[r] + q] : 0;
+                        rv[h] = q < rl ? a.rem_val[rstart[r] + q] : S(0);
+                    }
+#pragma unroll
+                    for (int h = 0; h < RG; ++h) {
+                        const int r = r0 + h;
+                        const int32_t sg = seg[r], bl = blen[r];
+                        const int32_t rl = last ? rlen[r] : 0;
+                        if (q < bl) lst[sg + q].val = bv[h];
+                        if (q < rl) lst[sg + bl + q] = make_entry<S>(rc[h], rv[h]);
+                    }
+                }
+            }
+#pragma unroll 1
+            for (int r = 0; r < BR; ++r) {   // row padding
+                const int32_t len = blen[r] + (last ? rlen[r] : 0);
                 const int32_t pad = (len + GR - 1) / GR * GR - len;
-                if (lane < pad) lst[sg + len + lane] = make_entry<S>(0, S(0));
+                if (lane < pad) lst[seg[r] + len + lane] = make_entry<S>(0, S(0));
             }
             __syncwarp();
+            if constexpr (NARROW) {
+                consume_narrow<S, BR, 32 / P>(lst, total, seg, 0, tile, c_lane, p_lane, lane_ok, Xb, a.K);
+                __syncwarp();
+                if (kc >= b1) break;
+                continue;
+            }
         }
 #pragma unroll 1
         for (int r = 0; r < BR; ++r) {
@@ -424,10 +529,24 @@ __device__ __forceinline__ void accumulate_rows(const StripeArgs<S>& a, S* tile,
                     while (rb) {
                         const int c = __ffs(rb) - 1;
                         rb &= rb - 1u;
-                        lst[pos++] = make_entry<S>(col0 + c, a.bdata[k++]);
+                        lst[pos++] = make_index_entry(col0 + c, k++, S(0));
                     }
                 }
                 n = blen[r];
+                __syncwarp();
+                for (int q0 = 0; q0 < n; q0 += 128) {   // the row's block values
+                    S v[4];
+#pragma unroll
+                    for (int h = 0; h < 4; ++h) {
+                        const int q = q0 + h * 32 + lane;
+                        v[h] = q < n ? a.bdata[entry_index(lst[q])] : S(0);
+                    }
+#pragma unroll
+                    for (int h = 0; h < 4; ++h) {
+                        const int q = q0 + h * 32 + lane;
+                        if (q < n) lst[q].val = v[h];
+                    }
+                }
                 if (last) {
                     rs = rstart[r];
                     re = rs + rlen[r];
@@ -443,7 +562,11 @@ __device__ __forceinline__ void accumulate_rows(const StripeArgs<S>& a, S* tile,
                     rs += take;
                     n = pad_list<S, GR>(lst, n, lane);
                 }
-                consume_list<S, V, P>(t, lst + base, n, Xb, a.K, p_lane);
+                if constexpr (NARROW) {
+                    consume_narrow<S, BR, 32 / P>(lst + base, n, nullptr, r, tile, c_lane, p_lane, lane_ok, Xb, a.K);
+                } else {
+                    consume_list<S, V, P>(t, lst + base, n, Xb, a.K, p_lane);
+                }
                 if (rs >= re) break;
                 __syncwarp();
                 n = 0;
@@ -452,7 +575,7 @@ __device__ __forceinline__ void accumulate_rows(const StripeArgs<S>& a, S* tile,
 #pragma unroll
                 for (int j = 0; j < V; ++j) t[j] += __shfl_xor_sync(0xffffffffu, t[j], 16);
             }
-            commit_row<S, V>(tile_lane, r, T, t, own);
+            if constexpr (!NARROW) commit_row<S, V>(tile_lane, r, T, t, own);
             if (!fits) __syncwarp();   // the next row reuses the list
         }
         __syncwarp();
@@ -461,17 +584,15 @@ __device__ __forceinline__ void accumulate_rows(const StripeArgs<S>& a, S* tile,
 }
 
 // Dynamic shared memory of one CTA of stripe_kernel, per warp: the output
-// tile [BR][T] (offset 0), then for P <= 2 the (column, value) list and the
-// row bookkeeping, or for P > 2 the staged X rows of one block per lane.
+// tile [BR][T] (offset 0), the (column, value) list and the row bookkeeping.
 template <typename S, int BR, int V, int C>
 struct StripeSmem {
     static constexpr int P = 32 / C;
     static constexpr int T = C * V;
     static constexpr size_t tile = (size_t)kStripeWarps * BR * T * sizeof(S);
-    static constexpr size_t list = P <= 2 ? (size_t)kStripeWarps * kListCap * sizeof(Entry<S>) : 0;
-    static constexpr size_t info = P <= 2 ? (size_t)kStripeWarps * 4 * BR * sizeof(int32_t) : 0;
-    static constexpr size_t stage = P > 2 ? (size_t)BR * kStripeThreads * V * sizeof(S) : 0;
-    static constexpr size_t bytes = tile + list + info + stage;
+    static constexpr size_t list = (size_t)kStripeWarps * kListCap * sizeof(Entry<S>);
+    static constexpr size_t info = (size_t)kStripeWarps * 4 * BR * sizeof(int32_t);
+    static constexpr size_t bytes = tile + list + info;
     static_assert(tile % 16 == 0 && list % 16 == 0, "regions stay 16-byte aligned");
 };
 
@@ -518,7 +639,6 @@ __global__ void __launch_bounds__(kStripeThreads, MinBlocks<S, V, PPR>::n)
 stripe_kernel(const StripeArgs<S> a) {
     constexpr int P = 32 / C;            // nonzero lanes per warp
     constexpr int T = C * V;             // columns per tile
-    constexpr uint32_t ROWMASK = (BC >= 32) ? 0xffffffffu : ((1u << BC) - 1u);
 
     using SM = StripeSmem<S, BR, V, C>;
     extern __shared__ __align__(16) unsigned char xs_dyn[];
@@ -527,7 +647,6 @@ stripe_kernel(const StripeArgs<S> a) {
     S* const otile = reinterpret_cast<S*>(xs_dyn) + (size_t)warp * BR * T;
     Entry<S>* const lst = reinterpret_cast<Entry<S>*>(xs_dyn + SM::tile) + (size_t)warp * kListCap;
     int32_t* const rowinfo = reinterpret_cast<int32_t*>(xs_dyn + SM::tile + SM::list) + (size_t)warp * 4 * BR;
-    Pack<S, V>* const xstage = reinterpret_cast<Pack<S, V>*>(xs_dyn + SM::tile);
 
     const int lane = threadIdx.x & 31;
     const int c_lane = lane % C;
@@ -583,22 +702,14 @@ stripe_kernel(const StripeArgs<S> a) {
         }
     };
 
-    // next work item: static round-robin first, then drawn from the counter
-    bool drawing = warp_id >= a.static_items;
-    auto draw = [&]() -> int64_t {
+    // next work item: drawn from the counter, or static round-robin
+    auto next_item = [&](int64_t cur) -> int64_t {
+        if (a.sched == nullptr) return cur + nwarps;
         unsigned long long v = 0;
         if (lane == 0) v = atomicAdd(a.sched, 1ull);
-        return a.static_items + (int64_t)__shfl_sync(0xffffffffu, v, 0);
+        return (int64_t)__shfl_sync(0xffffffffu, v, 0);
     };
-    auto next_item = [&](int64_t cur) -> int64_t {
-        if (!drawing) {
-            if (cur + nwarps < a.static_items) return cur + nwarps;
-            if (a.sched == nullptr) return items;
-            drawing = true;
-        }
-        return draw();
-    };
-    for (int64_t item = drawing ? (a.sched ? draw() : items) : warp_id; item < items; item = next_item(item)) {
+    for (int64_t item = a.sched != nullptr ? next_item(0) : warp_id; item < items; item = next_item(item)) {
         const int64_t u = item / BT;
         const int64_t bt = item - u * BT;
         const int64_t b = bt / a.ntiles;
@@ -632,7 +743,7 @@ stripe_kernel(const StripeArgs<S> a) {
             j1 = rj0 + (int32_t)r1;
         } else {
             s = u - a.num_pieces;
-            if (a.heavy_of != nullptr && a.heavy_of[s] >= 0) continue;
+            if (a.heavy_of != nullptr && a.heavy_of[s] >= 0) continue;   // done as pieces
             b0 = a.stripe_ptr[s];
             b1 = a.stripe_ptr[s + 1];
             const int64_t last_row = (s * BR + BR < a.rows) ? s * BR + BR : a.rows;
@@ -652,99 +763,8 @@ stripe_kernel(const StripeArgs<S> a) {
         // lanes past the last column read a valid address and never store
         const S* __restrict__ Xb = a.X + b * a.cols * (int64_t)a.K + (lane_ok ? col_base : 0);
 
-        if constexpr (P <= 2) {
-            accumulate_rows<S, BR, BC, V, P>(a, otile, lst, rowinfo, s, b0, b1, j0, j1, Xb, lane_ok, lane,
-                                             p_lane, c_lane);
-        } else {
-            S acc[BR][V];
-#pragma unroll
-            for (int r = 0; r < BR; ++r)
-#pragma unroll
-                for (int j = 0; j < V; ++j) acc[r][j] = S(0);
-            // ---- PBR blocks: lanes stride the blocks ------------------------
-            for (int32_t kb = b0 + p_lane; kb < b1; kb += P) {
-                const uint64_t code = static_cast<uint64_t>(a.codes[kb]);
-                const int64_t col0 = a.coords[2 * (int64_t)kb + 1];
-                int32_t k = a.offsets[kb];
-                uint32_t colmask = 0;
-#pragma unroll
-                for (int r = 0; r < BR; ++r) colmask |= (uint32_t)(code >> (r * BC)) & ROWMASK;
-                if (lane_ok) {
-#pragma unroll
-                    for (int c = 0; c < BC; ++c)
-                        if ((colmask >> c) & 1u)
-                            xstage[c * kStripeThreads + threadIdx.x] = load_pack<S, V>(Xb + (col0 + c) * a.K);
-                }
-#pragma unroll
-                for (int r = 0; r < BR; ++r) {
-                    uint32_t bits = (uint32_t)(code >> (r * BC)) & ROWMASK;
-                    while (bits) {
-                        const int c = __ffs(bits) - 1;
-                        bits &= bits - 1u;
-                        const S v = a.bdata[k++];
-                        if (lane_ok) {
-                            const Pack<S, V> x = xstage[c * kStripeThreads + threadIdx.x];
-#pragma unroll
-                            for (int j = 0; j < V; ++j) acc[r][j] = fma(v, x.v[j], acc[r][j]);
-                        }
-                    }
-                }
-            }
-            // ---- CSR remainder: lanes stride the entries of each row ---------
-#pragma unroll
-            for (int r = 0; r < BR; ++r) {
-                const int64_t row = s * BR + r;
-                if (row >= a.rows) continue;
-                int32_t rs = a.rem_ptr[row], re = a.rem_ptr[row + 1];
-                rs = rs > j0 ? rs : j0;
-                re = re < j1 ? re : j1;
-                int32_t jj = rs + p_lane;
-                for (; jj + 3 * P < re; jj += 4 * P) {
-                    const int64_t c0 = a.rem_col[jj], c1 = a.rem_col[jj + P];
-                    const int64_t c2 = a.rem_col[jj + 2 * P], c3 = a.rem_col[jj + 3 * P];
-                    const S v0 = a.rem_val[jj], v1 = a.rem_val[jj + P];
-                    const S v2 = a.rem_val[jj + 2 * P], v3 = a.rem_val[jj + 3 * P];
-                    if (lane_ok) {
-                        const Pack<S, V> x0 = load_pack<S, V>(Xb + c0 * a.K);
-                        const Pack<S, V> x1 = load_pack<S, V>(Xb + c1 * a.K);
-                        const Pack<S, V> x2 = load_pack<S, V>(Xb + c2 * a.K);
-                        const Pack<S, V> x3 = load_pack<S, V>(Xb + c3 * a.K);
-#pragma unroll
-                        for (int j = 0; j < V; ++j) {
-                            acc[r][j] = fma(v0, x0.v[j], acc[r][j]);
-                            acc[r][j] = fma(v1, x1.v[j], acc[r][j]);
-                            acc[r][j] = fma(v2, x2.v[j], acc[r][j]);
-                            acc[r][j] = fma(v3, x3.v[j], acc[r][j]);
-                        }
-                    }
-                }
-                for (; jj < re; jj += P) {
-                    const int64_t c0 = a.rem_col[jj];
-                    const S v0 = a.rem_val[jj];
-                    if (lane_ok) {
-                        const Pack<S, V> x0 = load_pack<S, V>(Xb + c0 * a.K);
-#pragma unroll
-                        for (int j = 0; j < V; ++j) acc[r][j] = fma(v0, x0.v[j], acc[r][j]);
-                    }
-                }
-            }
-            // ---- fold the P nonzero lanes into the tile ------------------------
-#pragma unroll
-            for (int off = C; off < 32; off <<= 1)
-#pragma unroll
-                for (int r = 0; r < BR; ++r)
-#pragma unroll
-                    for (int j = 0; j < V; ++j) acc[r][j] += __shfl_xor_sync(0xffffffffu, acc[r][j], off);
-            if (p_lane == 0 && lane_ok) {
-#pragma unroll
-                for (int r = 0; r < BR; ++r) {
-                    Pack<S, V> o;
-#pragma unroll
-                    for (int j = 0; j < V; ++j) o.v[j] = acc[r][j];
-                    store_pack<S, V>(otile + r * T + c_lane * V, o);
-                }
-            }
-        }
+        accumulate_rows<S, BR, BC, V, P>(a, otile, lst, rowinfo, s, b0, b1, j0, j1, Xb, lane_ok, lane, p_lane,
+                                         c_lane);
         // from here on lane (c_lane, p_lane == 0) owns columns [c_lane * V, +V)
         // of every tile row
 

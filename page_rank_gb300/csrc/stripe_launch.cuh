@@ -26,9 +26,6 @@ int launch_stripe_shape(const StripeArgs<S>& a0, cudaStream_t stream) {
     int64_t blocks = ceil_div(items, kStripeWarps);
     const int64_t cap = (int64_t)num_sms() * occ;
     if (blocks > cap) blocks = cap;
-    // the first GL_STATIC_PERCENT % of the items (whole rounds) go round-robin
-    const int64_t nwarps = blocks * kStripeWarps;
-    a.static_items = a.sched ? items * GL_STATIC_PERCENT / 100 / nwarps * nwarps : items;
     kern<<<(unsigned)blocks, kStripeThreads, smem, stream>>>(a);
     GL_LAUNCH_CHECK("stripe_kernel");
     return GL_OK;
