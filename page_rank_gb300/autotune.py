@@ -51,6 +51,9 @@ def autotune(A: sp.csr_matrix, K: int, device=None, candidates=None, steps: int 
         rng = np.random.default_rng(seed)
         seeds = torch.from_numpy(rng.integers(0, n, K).astype(np.int32)).to(dev)
         sptr = torch.arange(K + 1, dtype=torch.int32, device=dev)
+        gen = torch.Generator(device=dev).manual_seed(seed)
+        x_dense = torch.rand((n, K), generator=gen, device=dev)
+        x_dense /= x_dense.sum(dim=0, keepdim=True)
         table = []
         best = None
         for bs, mn, tile in (candidates or default_candidates(K)):
@@ -59,7 +62,9 @@ def autotune(A: sp.csr_matrix, K: int, device=None, candidates=None, steps: int 
             meta["column_tile"] = tile
             tp = teleport_from_seed_sets(sptr, seeds, n, bs)
             run = PprRun(meta, n, n, bs, bs, tp, alpha, steps + 2, 0.0, native.GL_PPR_STOP_ALL, dbits)
-            run.init()
+            # a dense start: mid-solve iterates are dense, and a step over
+            # them measured ~30 % slower than over the first, sparse ones
+            run.init(x_dense)
             run.launch_chunk(2)                      # warm (occupancy query, caches)
             torch.cuda.synchronize(dev)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
