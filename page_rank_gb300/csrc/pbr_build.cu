@@ -82,6 +82,11 @@ struct BuildWs {
     int32_t*  rec_v0;
     int32_t*  rec_k1;
     int32_t*  rec_v1;
+    // big stripes: per-entry sort / scan scratch, indexed by CSR position
+    int32_t*  ent_a;
+    int32_t*  ent_b;
+    int32_t*  ent_c;
+    int32_t*  ent_d;
     int64_t bytes;
 };
 
@@ -115,6 +120,10 @@ BuildWs layout_ws(void* base, int64_t rows, int64_t nnz, int32_t br) {
     w.rec_v0 = reinterpret_cast<int32_t*>(take(4 * nr));
     w.rec_k1 = reinterpret_cast<int32_t*>(take(4 * nr));
     w.rec_v1 = reinterpret_cast<int32_t*>(take(4 * nr));
+    w.ent_a = reinterpret_cast<int32_t*>(take(4 * nr));
+    w.ent_b = reinterpret_cast<int32_t*>(take(4 * nr));
+    w.ent_c = reinterpret_cast<int32_t*>(take(4 * nr));
+    w.ent_d = reinterpret_cast<int32_t*>(take(4 * nr));
     w.bytes = off;
     return w;
 }
@@ -198,6 +207,21 @@ struct StripeMerge {
     }
 };
 
+// Entries of stripe s according to indptr (clamped to [0, nnz]).
+template <typename I>
+__device__ __forceinline__ int64_t stripe_entries(const I* indptr, int64_t s, int64_t rows, int64_t nnz, int br) {
+    const int64_t r0 = s * br;
+    const int64_t r1 = r0 + br < rows ? r0 + br : rows;
+    int64_t a = (int64_t)indptr[r0], b = (int64_t)indptr[r1];
+    a = a < 0 ? 0 : (a > nnz ? nnz : a);
+    b = b < a ? a : (b > nnz ? nnz : b);
+    return b - a;
+}
+
+// Stripes with more entries than this are counted by a whole CTA
+// (build_count_big_kernel) instead of one warp's serial merge.
+constexpr int64_t kBigCountEntries = 2048;
+
 // ---------------------------------------------------------------------------
 // count: per stripe distinct / kept blocks and kept values; per row remainder
 // entries; validation flags.
@@ -210,6 +234,7 @@ build_count_kernel(const I* indptr, const I* indices, int64_t rows, int64_t cols
     const int64_t warp_id = (int64_t)blockIdx.x * kBuildWarps + (threadIdx.x >> 5);
     const int64_t nwarps = (int64_t)gridDim.x * kBuildWarps;
     for (int64_t s = warp_id; s < nstripes; s += nwarps) {
+        if (stripe_entries(indptr, s, rows, nnz, br) > kBigCountEntries) continue;   // build_count_big_kernel
         StripeMerge<I> mg;
         mg.init(indptr, indices, s, rows, nnz, br, bc, true);
         int64_t m = 0, kept = 0, packed = 0, rem = 0;
@@ -369,6 +394,8 @@ __device__ void move_values(const I* indptr, const I* indices, const S* values, 
 //     popcounts in list order.
 // ---------------------------------------------------------------------------
 struct BigShared {
+    int32_t rowstart[33];                  // stripe-local row starts (block_rows + 1)
+    int32_t nruns;
     int32_t hist[256];                     // digit bases of the pass
     int32_t tile_tot[256];                 // digit counts of the tile
     int32_t wcnt[kBigThreads / 32][256];   // per-warp digit counts, then prefixes
@@ -544,6 +571,204 @@ __device__ void list_order_big(BigShared& sh, int64_t s, int64_t ncb, bool key32
     __syncthreads();
 }
 
+// Stripe-local row of entry i (rowstart[0..br] in shared memory).
+__device__ __forceinline__ int big_row_of(const BigShared& sh, int br, int i) {
+    int lo = 0, hi = br;   // rowstart[lo] <= i < rowstart[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (sh.rowstart[mid] <= i) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// The stripe's entries, stable-sorted by block column: sorted keys in a,
+// stripe-local entry indices (CSR order) in b; c / d are scratch.
+struct BigEntries {
+    int32_t* a;
+    int32_t* b;
+    int32_t* c;
+    int32_t* d;
+};
+
+// record_blocks for a big stripe, one 1024-thread CTA: the stripe's entries
+// are stable-sorted by block column, so each run of equal block columns is
+// one distinct block with its entries in CSR (= row-major bit) order; the
+// run's first entry is the block's first CSR position.  Leaves the sorted
+// entries, the run index + 1 of each sorted entry (c) and each run's first
+// sorted position (d) for move_values_big.
+template <typename I>
+__device__ void record_blocks_big(BigShared& sh, const I* indptr, const I* indices, int64_t s, int64_t rows,
+                                  int br, int bc, int64_t ncb, const BigEntries& en, uint64_t* code_r,
+                                  int64_t* bcol_r, int32_t* first_r) {
+    const int t = threadIdx.x;
+    const int64_t r0 = s * br;
+    const int64_t r1 = r0 + br < rows ? r0 + br : rows;
+    const int64_t e0 = (int64_t)indptr[r0];
+    const int n = (int)((int64_t)indptr[r1] - e0);
+    if (t <= br) sh.rowstart[t] = (int32_t)((int64_t)indptr[r0 + t < r1 ? r0 + t : r1] - e0);
+    for (int i = t; i < n; i += kBigThreads) {
+        en.a[i] = (int32_t)((int64_t)indices[e0 + i] / bc);
+        en.b[i] = i;
+    }
+    __syncthreads();
+    const int bits = 64 - __clzll((long long)(ncb > 1 ? ncb - 1 : 1));
+    big_sort(sh, en.a, en.b, en.c, en.d, n, bits);
+    for (int p = t; p < n; p += kBigThreads) en.c[p] = (p == 0 || en.a[p] != en.a[p - 1]) ? 1 : 0;
+    __syncthreads();
+    big_scan<false>(sh, en.c, n, true);   // run index + 1
+    for (int p = t; p < n; p += kBigThreads) {
+        if (p == 0 || en.a[p] != en.a[p - 1]) {
+            const int j = en.c[p] - 1;
+            en.d[j] = p;
+            bcol_r[j] = en.a[p];
+            first_r[j] = en.b[p];
+            code_r[j] = 0;
+        }
+    }
+    __syncthreads();
+    for (int p = t; p < n; p += kBigThreads) {
+        const int i = en.b[p];
+        const int r = big_row_of(sh, br, i);
+        const int64_t col = (int64_t)indices[e0 + i];
+        atomicOr(reinterpret_cast<unsigned long long*>(code_r + (en.c[p] - 1)), 1ull << (r * bc + (int)(col % bc)));
+    }
+    __syncthreads();
+}
+
+// move_values for a big stripe (after record_blocks_big and the ordering):
+// kept blocks' entries go straight to block_data at the block's value offset
+// plus their rank in the run; the others go to their row's remainder at the
+// row's offset plus their rank among the row's dropped entries (an inclusive
+// scan of drop flags in CSR order).
+template <typename I, typename S>
+__device__ void move_values_big(BigShared& sh, const I* indptr, const I* indices, const S* values, int64_t s,
+                                int64_t rows, int br, const BigEntries& en, const int32_t* slot,
+                                const int32_t* doff, int64_t packed_base, const int64_t* row_rem, S* out_data,
+                                I* out_rem_col, S* out_rem_val) {
+    const int t = threadIdx.x;
+    const int64_t r0 = s * br;
+    const int64_t r1 = r0 + br < rows ? r0 + br : rows;
+    const int64_t e0 = (int64_t)indptr[r0];
+    const int n = (int)((int64_t)indptr[r1] - e0);
+    for (int p = t; p < n; p += kBigThreads) {
+        const int j = en.c[p] - 1;
+        const int i = en.b[p];
+        const int sl = slot[j];
+        if (sl >= 0) out_data[packed_base + doff[j] + (p - en.d[j])] = values[e0 + i];
+        en.a[i] = sl < 0 ? 1 : 0;
+    }
+    __syncthreads();
+    big_scan<false>(sh, en.a, n, true);
+    for (int i = t; i < n; i += kBigThreads) {
+        const int32_t before = i > 0 ? en.a[i - 1] : 0;
+        if (en.a[i] == before) continue;   // kept
+        const int r = big_row_of(sh, br, i);
+        const int rs = sh.rowstart[r];
+        const int32_t row_before = rs > 0 ? en.a[rs - 1] : 0;
+        const int64_t dst = row_rem[r0 + r] + (before - row_before);
+        out_rem_col[dst] = indices[e0 + i];
+        out_rem_val[dst] = values[e0 + i];
+    }
+    __syncthreads();
+}
+
+// count for a stripe with more than kBigCountEntries entries, one
+// 1024-thread CTA: validation of its rows, then a stable sort of its
+// entries by block column; runs are the distinct blocks, their codes are
+// OR-ed together (two 32-bit halves), and kept blocks, packed values and
+// per-row remainder entries are summed.
+template <typename I>
+__global__ void __launch_bounds__(kBigThreads)
+build_count_big_kernel(const I* indptr, const I* indices, int64_t rows, int64_t cols, int64_t nnz, int br, int bc,
+                       int min_nnz, int64_t nstripes, int64_t ncb, BuildWs w) {
+    __shared__ BigShared sh;
+    __shared__ unsigned long long s_tot[3];   // distinct, kept, packed
+    __shared__ int32_t s_rem[33];
+    __shared__ int32_t s_bad[3];
+    const int t = threadIdx.x;
+    for (int64_t s = blockIdx.x; s < nstripes; s += gridDim.x) {
+        if (stripe_entries(indptr, s, rows, nnz, br) <= kBigCountEntries) continue;
+        const int64_t r0 = s * br;
+        const int64_t r1 = r0 + br < rows ? r0 + br : rows;
+        const int nr = (int)(r1 - r0);
+        int64_t e0 = (int64_t)indptr[r0];
+        e0 = e0 < 0 ? 0 : (e0 > nnz ? nnz : e0);
+        const int n = (int)stripe_entries(indptr, s, rows, nnz, br);
+        if (t < 3) {
+            s_tot[t] = 0;
+            s_bad[t] = 0;
+        }
+        if (t <= br) s_rem[t] = 0;
+        if (t < nr) {   // the rows' indptr
+            const int64_t row = r0 + t;
+            const int64_t a = (int64_t)indptr[row], b = (int64_t)indptr[row + 1];
+            if (a < 0 || b < a || b > nnz || (row == 0 && a != 0) || (row + 1 == rows && b != nnz)) s_bad[kFlagIndptr] = 1;
+        }
+        if (t <= br) {
+            int64_t v = (int64_t)indptr[r0 + t < r1 ? r0 + t : r1] - e0;
+            v = v < 0 ? 0 : (v > n ? n : v);
+            sh.rowstart[t] = (int32_t)v;
+        }
+        __syncthreads();
+        BigEntries en{w.ent_a + e0, w.ent_b + e0, w.ent_c + e0, w.ent_d + e0};
+        for (int i = t; i < n; i += kBigThreads) {
+            int64_t col = (int64_t)indices[e0 + i];
+            const int r = big_row_of(sh, br, i);
+            if (col < 0 || col >= cols) s_bad[kFlagRange] = 1;
+            if (i > sh.rowstart[r] && col <= (int64_t)indices[e0 + i - 1]) s_bad[kFlagNoncanon] = 1;
+            col = col < 0 ? 0 : (col >= cols ? cols - 1 : col);
+            en.a[i] = (int32_t)(col / bc);
+            en.b[i] = i;
+        }
+        __syncthreads();
+        const int bits = 64 - __clzll((long long)(ncb > 1 ? ncb - 1 : 1));
+        big_sort(sh, en.a, en.b, en.c, en.d, n, bits);
+        for (int p = t; p < n; p += kBigThreads) en.c[p] = (p == 0 || en.a[p] != en.a[p - 1]) ? 1 : 0;
+        __syncthreads();
+        big_scan<false>(sh, en.c, n, true);   // run index + 1
+        const int m = n > 0 ? en.c[n - 1] : 0;
+        for (int j = t; j < m; j += kBigThreads) {   // codes: low half in a, high half in d
+            en.a[j] = 0;
+            en.d[j] = 0;
+        }
+        __syncthreads();
+        for (int p = t; p < n; p += kBigThreads) {
+            const int i = en.b[p];
+            const int r = big_row_of(sh, br, i);
+            int64_t col = (int64_t)indices[e0 + i];
+            col = col < 0 ? 0 : (col >= cols ? cols - 1 : col);
+            const int bit = r * bc + (int)(col % bc);
+            if (bit < 32) atomicOr(reinterpret_cast<unsigned*>(en.a + (en.c[p] - 1)), 1u << bit);
+            else atomicOr(reinterpret_cast<unsigned*>(en.d + (en.c[p] - 1)), 1u << (bit - 32));
+        }
+        __syncthreads();
+        for (int j = t; j < m; j += kBigThreads) {
+            const int pop = __popc((unsigned)en.a[j]) + __popc((unsigned)en.d[j]);
+            atomicAdd(&s_tot[0], 1ull);
+            if (pop >= min_nnz) {
+                atomicAdd(&s_tot[1], 1ull);
+                atomicAdd(&s_tot[2], (unsigned long long)pop);
+            }
+        }
+        for (int p = t; p < n; p += kBigThreads) {
+            const int j = en.c[p] - 1;
+            const int pop = __popc((unsigned)en.a[j]) + __popc((unsigned)en.d[j]);
+            if (pop < min_nnz) atomicAdd(&s_rem[big_row_of(sh, br, en.b[p])], 1);
+        }
+        __syncthreads();
+        if (t == 0) {
+            w.stripe_m[s] = (int64_t)s_tot[0];
+            w.stripe_kept[s] = (int64_t)s_tot[1];
+            w.stripe_packed[s] = (int64_t)s_tot[2];
+            for (int f = 0; f < 3; ++f)
+                if (s_bad[f]) atomicOr(&w.flags[f], 1);
+        }
+        if (t < nr) w.row_rem[r0 + t] = s_rem[t];
+        __syncthreads();
+    }
+}
+
 // order_stripe for a big stripe (one 1024-thread CTA; see the section
 // comment above).  Same outputs as order_stripe.
 template <typename I>
@@ -696,19 +921,17 @@ build_fill_big_kernel(const I* indptr, const I* indices, const S* values, int64_
         const int64_t rbase = w.stripe_m[s];
         const int m = (int)(w.stripe_m[s + 1] - rbase);
         if (m <= kSmallStripeBlocks) continue;
-        if (threadIdx.x < 32)
-            record_blocks<I>(indptr, indices, s, rows, cols, nnz, br, bc, w.rec_code + rbase, w.rec_bcol + rbase,
+        const int64_t e0 = (int64_t)indptr[s * br];
+        BigEntries en{w.ent_a + e0, w.ent_b + e0, w.ent_c + e0, w.ent_d + e0};
+        record_blocks_big<I>(sh, indptr, indices, s, rows, br, bc, ncb, en, w.rec_code + rbase, w.rec_bcol + rbase,
                              w.rec_ins + rbase);
-        __syncthreads();
         BigRecs r{w.rec_code + rbase, w.rec_bcol + rbase, w.rec_ins + rbase, w.rec_tau + rbase,
                   w.rec_bkt + rbase, w.rec_g + rbase, w.rec_pos + rbase, w.rec_pops + rbase,
                   w.rec_k0 + rbase, w.rec_v0 + rbase, w.rec_k1 + rbase, w.rec_v1 + rbase};
         order_stripe_big<I>(sh, s, m, br, bc, min_nnz, ncb, key32, nchain, w.chain, w.stripe_prefmax[s],
                             w.stripe_kept[s], w.stripe_packed[s], r, out_codes, out_coords, out_offsets);
-        if (threadIdx.x < 32)
-            move_values<I, S>(indptr, indices, values, s, rows, cols, nnz, br, bc, w.rec_tau + rbase,
-                              w.rec_g + rbase, w.stripe_packed[s], w.row_rem, out_data, out_rem_col, out_rem_val);
-        __syncthreads();
+        move_values_big<I, S>(sh, indptr, indices, values, s, rows, br, en, w.rec_tau + rbase, w.rec_g + rbase,
+                              w.stripe_packed[s], w.row_rem, out_data, out_rem_col, out_rem_val);
     }
 }
 
@@ -777,6 +1000,12 @@ int count_impl(const I* indptr, const I* indices, int64_t rows, int64_t cols, in
         build_count_kernel<I><<<(unsigned)blocks, kBuildThreads, 0, stream>>>(indptr, indices, rows, cols, nnz, br,
                                                                               bc, min_nnz, ns, w);
         GL_LAUNCH_CHECK("build_count_kernel");
+        const int64_t ncb = ceil_div(cols, bc);
+        int64_t big_blocks = (int64_t)num_sms() * 2;
+        if (big_blocks > ns) big_blocks = ns;
+        build_count_big_kernel<I><<<(unsigned)big_blocks, kBigThreads, 0, stream>>>(indptr, indices, rows, cols, nnz,
+                                                                                    br, bc, min_nnz, ns, ncb, w);
+        GL_LAUNCH_CHECK("build_count_big_kernel");
     }
     int rc;
     // exclusive running max of distinct blocks per stripe (bucket state)

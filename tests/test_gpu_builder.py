@@ -119,3 +119,38 @@ def test_builder_hub_stripes_vs_oracle(device):
         want = oracle.csr_to_pbr(A.indptr, A.indices, A.data, n, A.shape[1], br, br, mn)
         _, got = _gpu(A, br, br, mn)
         assert_pbr_equal(got, want, f"hub b={br} min={mn}")
+
+
+@pytest.mark.parametrize("rows_per_stripe", [2, 8])
+def test_builder_validation_in_long_stripes(rows_per_stripe, device):
+    """Out-of-range, unsorted and duplicate columns inside stripes long
+    enough for the CTA-parallel count are rejected with the same statuses
+    as in short ones."""
+    import torch
+
+    from page_rank_gb300 import native
+    from page_rank_gb300.pbr import build_pbr_device
+    dense = sp.random(16, 30000, density=0.3, format="csr", dtype=np.float32, random_state=3)
+    dense.sort_indices()
+    ip = torch.from_numpy(dense.indptr.astype(np.int32)).to(device)
+    dv = torch.from_numpy(dense.data).to(device)
+    good = dense.indices.astype(np.int32)
+    assert np.diff(dense.indptr).max() * rows_per_stripe > 2048
+    build_pbr_device(ip, torch.from_numpy(good).to(device), dv, 16, 30000, rows_per_stripe, rows_per_stripe, 1)
+    k = int(dense.indptr[3]) + 100           # an entry in the middle of row 3
+    bad_range = good.copy()
+    bad_range[k] = 30000 + 5
+    with pytest.raises(native.GLValueError, match="out of range"):
+        build_pbr_device(ip, torch.from_numpy(bad_range).to(device), dv, 16, 30000, rows_per_stripe,
+                         rows_per_stripe, 1)
+    for bad in (good.copy(), good.copy()):
+        bad[k], bad[k + 1] = bad[k + 1], bad[k]
+        break
+    unsorted = bad
+    dup = good.copy()
+    dup[k + 1] = dup[k]
+    for arr in (unsorted, dup):
+        with pytest.raises(native.GLError) as ei:
+            build_pbr_device(ip, torch.from_numpy(arr).to(device), dv, 16, 30000, rows_per_stripe,
+                             rows_per_stripe, 1)
+        assert ei.value.code == native.GL_ERR_NONCANONICAL
