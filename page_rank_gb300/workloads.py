@@ -116,7 +116,18 @@ def warmstart(device, log2n: int = 21, train_vectors: int = 20000, K: int = 256)
 
 
 def serving(device, rates=(200.0, 800.0, 3200.0), requests_per_rate: int = 400, graphs: int = 8,
-            warm: bool = True, seed: int = 5) -> dict:
+            seed: int = 5) -> dict:
+    """The serving configuration with the learned warm start on (as the
+    configuration asks) and, for comparison, off."""
+    on = serving_pass(device, rates, requests_per_rate, graphs, True, seed)
+    off = serving_pass(device, rates, requests_per_rate, graphs, False, seed)
+    return {"workload": on["workload"].replace(", warm start on", ""), "resident_bytes": on["resident_bytes"],
+            "warm_start_on": {"rates": on["rates"], "admission_waits": on["admission_waits"]},
+            "warm_start_off": {"rates": off["rates"], "admission_waits": off["admission_waits"]}}
+
+
+def serving_pass(device, rates=(200.0, 800.0, 3200.0), requests_per_rate: int = 400, graphs: int = 8,
+                 warm: bool = True, seed: int = 5) -> dict:
     """8 resident cluster / Zipf graphs with n log-uniform in 2**16 .. 2**22,
     Poisson arrivals at each rate, 1-64 seeds per request, alpha in
     {0.8, 0.85, 0.9}, certified L1 1e-6; p50 / p99 latency and queries/s."""
