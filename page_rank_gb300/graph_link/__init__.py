@@ -24,6 +24,7 @@ from .. import native
 from ..pbr import (DataOrder, PBRMatrix, PBRMatrixInt32Double, PBRMatrixInt32Float,
                    PBRMatrixInt64Double, PBRMatrixInt64Float, matrix_desc, pbr_from_device_csr,
                    spmm_workspace)
+from ..pbr_io import load_pbr, save_pbr
 from ..ppr import PprRun, dangling_bitmap, teleport_from_seed_sets
 from .pbr_registry import clear_pbr_gpu_meta, get_pbr_gpu_meta, set_pbr_gpu_meta
 
@@ -268,6 +269,8 @@ __all__ = [
     "run_personalized_pagerank",
     "clear_pbr_gpu_meta",
     "DataOrder",
+    "save_pbr",
+    "load_pbr",
     "PBRMatrixInt32Float",
     "PBRMatrixInt64Float",
     "PBRMatrixInt32Double",
