@@ -139,17 +139,22 @@ class PPREngine:
 
     def solve(self, seed_sets, alpha: float = 0.85, tol: float = 1e-6, max_iterations: int = 1000,
               certified: bool = True, retire: bool = True, chunk: int = 8, x0: torch.Tensor | None = None,
-              use_graphs: bool = True, compact_ratio: float = 0.75) -> BatchResult:
+              use_graphs: bool = True, compact_ratio: float = 0.75, warm_start=None) -> BatchResult:
         """Personalized PageRank for every seed set (one column each).
 
         ``certified`` stops a column once its update is below
         ``certified_tolerance(tol, alpha)`` so its distance to the exact fixed
         point is at most ``tol`` in L1; otherwise the update itself is compared
-        with ``tol`` (the reference's rule)."""
+        with ``tol`` (the reference's rule).  ``warm_start`` (a trained
+        ``warmstart.WarmStart`` of this engine) supplies the start columns
+        when ``x0`` is not given; the fixed point is the same."""
         K = len(seed_sets)
         dev = self.device
+        t0 = time.perf_counter()   # the solve's time includes the warm start's prediction
+        warm_columns = None
+        if warm_start is not None and x0 is None:
+            x0, warm_columns = warm_start.start_vectors(seed_sets, alpha)
         thr = certified_tolerance(tol, alpha) if certified else tol
-        t0 = time.perf_counter()
         with torch.cuda.device(dev):
             ptr, rows, w = self.teleport(seed_sets)
             out = torch.empty((self.n, K), dtype=torch.float32, device=dev)
@@ -215,9 +220,12 @@ class PPREngine:
                 else:
                     active = active[:0]
             torch.cuda.synchronize(dev)
-        return BatchResult(X=out, iterations=col_iter, launched_iterations=launched,
-                           converged=col_iter >= 0, seconds=time.perf_counter() - t0,
-                           column_steps=column_steps, history=history)
+        res = BatchResult(X=out, iterations=col_iter, launched_iterations=launched,
+                          converged=col_iter >= 0, seconds=time.perf_counter() - t0,
+                          column_steps=column_steps, history=history)
+        if warm_columns is not None:
+            res.warm_columns = warm_columns
+        return res
 
     def solve_plain(self, seed_sets, alpha: float = 0.85, tol: float = 1e-6, max_iterations: int = 1000,
                     certified: bool = True) -> BatchResult:

@@ -217,12 +217,7 @@ class PPRServer:
         with torch.cuda.stream(stream):
             if ws is None:
                 return eng.teleport_columns(seed_sets)
-            x_warm = ws.predict(seed_sets)
-            V = ws.seed_matrix(seed_sets)
-            r_w = ws.first_residual(seed_sets, x_warm, alpha)
-            r_c = ws.first_residual(seed_sets, V, alpha)
-            use = torch.from_numpy(r_w < r_c).to(self.device)[None, :]
-            return torch.where(use, x_warm, V)
+            return ws.start_vectors(seed_sets, alpha)[0]
 
     # -- requests -----------------------------------------------------------------
     def submit(self, graph: str, seeds, alpha: float = 0.85, tol: float = 1e-6,

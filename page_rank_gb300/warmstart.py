@@ -238,17 +238,19 @@ class WarmStart:
                 out[:, c0 + k] = x / x.sum()
         return out
 
-    def solve(self, seed_sets, alpha: float = 0.85, tol: float = 1e-6, max_iterations: int = 1000, **kw):
-        """Warm-started batched solve with per-column fallback to the cold start."""
+    def start_vectors(self, seed_sets, alpha) -> tuple[torch.Tensor, np.ndarray]:
+        """Start columns: the prediction where its first residual is below the
+        cold start's, else the teleport vector; and which columns use it."""
         x_warm = self.predict(seed_sets)
         V = self.seed_matrix(seed_sets)
         r_warm = self.first_residual(seed_sets, x_warm, alpha)
         r_cold = self.first_residual(seed_sets, V, alpha)
         use_warm = r_warm < r_cold
-        x0 = torch.where(torch.from_numpy(use_warm).to(self.dev)[None, :], x_warm, V)
-        res = self.eng.solve(seed_sets, alpha=alpha, tol=tol, max_iterations=max_iterations, x0=x0, **kw)
-        res.warm_columns = use_warm
-        return res
+        return torch.where(torch.from_numpy(use_warm).to(self.dev)[None, :], x_warm, V), use_warm
+
+    def solve(self, seed_sets, alpha: float = 0.85, tol: float = 1e-6, max_iterations: int = 1000, **kw):
+        """Warm-started batched solve with per-column fallback to the cold start."""
+        return self.eng.solve(seed_sets, alpha=alpha, tol=tol, max_iterations=max_iterations, warm_start=self, **kw)
 
     def first_residual(self, seed_sets, x0: torch.Tensor, alpha: float) -> np.ndarray:
         """||P(x0) - x0||_1 per column (one fused step)."""
