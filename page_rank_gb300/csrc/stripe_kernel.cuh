@@ -131,6 +131,43 @@ __device__ __forceinline__ void store_pack(S* p, const Pack<S, V>& v) {
     *reinterpret_cast<Pack<S, V>*>(p) = v;
 }
 
+// X-row gather: a plain load (GL_GATHER_LOAD 0), L2 only (1), or read-only
+// without L1 allocation (2).  The L1 catches a fifth of the gathers and
+// either bypass measured ~55 % slower, so 0 stays.
+#ifndef GL_GATHER_LOAD
+#define GL_GATHER_LOAD 0
+#endif
+template <typename S, int V>
+__device__ __forceinline__ Pack<S, V> gather_pack(const S* p) {
+#if GL_GATHER_LOAD == 1
+    Pack<S, V> r;
+    if constexpr (sizeof(S) * V == 16) {
+        const float4 v = __ldcg(reinterpret_cast<const float4*>(p));
+        static_assert(sizeof(r) == sizeof(v), "pack size");
+        memcpy(&r, &v, sizeof(v));
+    } else if constexpr (sizeof(S) * V == 8) {
+        const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+        memcpy(&r, &v, sizeof(v));
+    } else {
+        r = load_pack_cg<S, V>(p);
+    }
+    return r;
+#elif GL_GATHER_LOAD == 2
+    Pack<S, V> r;
+    if constexpr (sizeof(S) * V == 16) {
+        float4 v;
+        asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+                     : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+        memcpy(&r, &v, sizeof(v));
+    } else {
+        r = load_pack<S, V>(p);
+    }
+    return r;
+#else
+    return load_pack<S, V>(p);
+#endif
+}
+
 // First index in [lo, hi) with offsets[idx] >= key (hi if none).
 __device__ __forceinline__ int32_t lower_bound_i32(const int32_t* offsets, int32_t lo, int32_t hi, int64_t key) {
     while (lo < hi) {
@@ -147,7 +184,13 @@ __device__ __forceinline__ int32_t lower_bound_i32(const int32_t* offsets, int32
 // loads, one address and V FMAs per nonzero, with the gathers of a batch all
 // in flight before the first FMA.
 // ---------------------------------------------------------------------------
-constexpr int kListCap = 384;     // entries per warp list (a unit that does not fit goes row by row)
+#ifndef GL_LIST_CAP
+#define GL_LIST_CAP 288
+#endif
+// entries per warp list (a chunk that does not fit goes row by row); small,
+// because shared memory left unused goes to the L1 that catches repeated X
+// rows (288 measured 2-7 % faster than 384, 512 slower)
+constexpr int kListCap = GL_LIST_CAP;
 // X-row gathers in flight per warp in the main batch (half that for 16-byte
 // lanes); row tails go in batches of kTail
 #ifndef GL_GATHER_DEPTH
@@ -213,8 +256,8 @@ __device__ __forceinline__ void gather_batch(S (&t)[V], const Entry<S>* lst, int
 #pragma unroll
         for (int q = 0; q < NB; q += 2) {
             const int4 c = w[q / 2];
-            x[q] = load_pack<S, V>(Xb + (long long)c.x * K);
-            x[q + 1] = load_pack<S, V>(Xb + (long long)c.z * K);
+            x[q] = gather_pack<S, V>(Xb + (long long)c.x * K);
+            x[q + 1] = gather_pack<S, V>(Xb + (long long)c.z * K);
         }
 #pragma unroll
         for (int q = 0; q < NB; q += 2) {
@@ -227,7 +270,7 @@ __device__ __forceinline__ void gather_batch(S (&t)[V], const Entry<S>* lst, int
         }
     } else {
 #pragma unroll
-        for (int q = 0; q < NB; ++q) x[q] = load_pack<S, V>(Xb + (long long)lst[e + q * P].col * K);
+        for (int q = 0; q < NB; ++q) x[q] = gather_pack<S, V>(Xb + (long long)lst[e + q * P].col * K);
 #pragma unroll
         for (int q = 0; q < NB; ++q) {
             const S v = lst[e + q * P].val;
