@@ -409,7 +409,7 @@ template <typename S, int BR, int BC, int V, int P>
 __device__ __forceinline__ void accumulate_rows(const StripeArgs<S>& a, S* tile, Entry<S>* lst, int32_t* rowinfo,
                                                 int64_t s, int32_t b0, int32_t b1, int32_t j0, int32_t j1,
                                                 const S* __restrict__ Xb, bool lane_ok, int lane, int p_lane,
-                                                int c_lane) {
+                                                int c_lane, bool rp_known, int32_t rp) {
     constexpr uint32_t ROWMASK = (BC >= 32) ? 0xffffffffu : ((1u << BC) - 1u);
     constexpr bool NARROW = P > 2;
     constexpr int GR = NARROW ? 1 : kTail * P;   // row granule
@@ -422,14 +422,16 @@ __device__ __forceinline__ void accumulate_rows(const StripeArgs<S>& a, S* tile,
     const bool own = (p_lane == 0) && lane_ok;
     S* tile_lane = tile + c_lane * V;
 
-    // remainder row ranges of this unit (lane r computes row r); zero the tile
+    // remainder row ranges of this unit (lane r computes row r; rp_known:
+    // lane r already holds rem_ptr of row r); zero the tile
     __syncwarp();
+    const int32_t rp_next = __shfl_down_sync(0xffffffffu, rp, 1);
     if (lane < BR) {
         const int64_t row = s * BR + lane;
         int32_t rs = j1, re = j1;
         if (row < a.rows) {
-            rs = a.rem_ptr[row];
-            re = a.rem_ptr[row + 1];
+            rs = rp_known ? rp : a.rem_ptr[row];
+            re = rp_known ? rp_next : a.rem_ptr[row + 1];
             rs = rs > j0 ? rs : j0;
             re = re < j1 ? re : j1;
             re = re > rs ? re : rs;
@@ -515,7 +517,10 @@ __device__ __forceinline__ void accumulate_rows(const StripeArgs<S>& a, S* tile,
                 const int32_t l = blen[r] > (last ? rlen[r] : 0) ? blen[r] : (last ? rlen[r] : 0);
                 longest = l > longest ? l : longest;
             }
-            constexpr int RG = BR < 4 ? BR : 4;   // rows whose loads are in flight together
+#ifndef GL_FETCH_ROWS
+#define GL_FETCH_ROWS 4
+#endif
+            constexpr int RG = BR < GL_FETCH_ROWS ? BR : GL_FETCH_ROWS;   // rows whose loads fly together
             for (int j0 = 0; j0 < longest; j0 += 32) {
                 const int q = j0 + lane;
 #pragma unroll
@@ -764,6 +769,8 @@ stripe_kernel(const StripeArgs<S> a) {
         int64_t s;
         int32_t b0, b1, j0, j1;
         int32_t h = -1, pidx = 0, npieces = 1;
+        int32_t rp = 0;            // lane r <= BR: rem_ptr of the stripe's row r
+        bool rp_known = false;
         if (u < a.num_pieces) {
             h = a.piece_heavy[u];
             s = a.heavy_stripe[h];
@@ -785,13 +792,19 @@ stripe_kernel(const StripeArgs<S> a) {
             j0 = rj0 + (int32_t)r0;
             j1 = rj0 + (int32_t)r1;
         } else {
+            // every load of the stripe's setup issued before the first use
+            // (one memory round trip): heavy flag, block range, and the
+            // remainder row pointers, lane r holding row r's
             s = u - a.num_pieces;
-            if (a.heavy_of != nullptr && a.heavy_of[s] >= 0) continue;   // done as pieces
+            const int nr = (int)(s * BR + BR < a.rows ? BR : a.rows - s * BR);
+            const int32_t hv = a.heavy_of != nullptr ? a.heavy_of[s] : -1;
             b0 = a.stripe_ptr[s];
             b1 = a.stripe_ptr[s + 1];
-            const int64_t last_row = (s * BR + BR < a.rows) ? s * BR + BR : a.rows;
-            j0 = a.rem_ptr[s * BR];
-            j1 = a.rem_ptr[last_row];
+            if (lane <= nr) rp = a.rem_ptr[s * BR + lane];
+            if (hv >= 0) continue;   // done as pieces
+            j0 = __shfl_sync(0xffffffffu, rp, 0);
+            j1 = __shfl_sync(0xffffffffu, rp, nr);
+            rp_known = true;
         }
 
         if constexpr (PPR) {
@@ -807,7 +820,7 @@ stripe_kernel(const StripeArgs<S> a) {
         const S* __restrict__ Xb = a.X + b * a.cols * (int64_t)a.K + (lane_ok ? col_base : 0);
 
         accumulate_rows<S, BR, BC, V, P>(a, otile, lst, rowinfo, s, b0, b1, j0, j1, Xb, lane_ok, lane, p_lane,
-                                         c_lane);
+                                         c_lane, rp_known, rp);
         // from here on lane (c_lane, p_lane == 0) owns columns [c_lane * V, +V)
         // of every tile row
 
