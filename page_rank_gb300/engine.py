@@ -248,19 +248,7 @@ class PPREngine:
 
     def _capture(self, run: PprRun, chunk: int):
         """CUDA graph of one chunk of steps for this run's buffers."""
-        s = torch.cuda.Stream(self.device)
-        s.wait_stream(torch.cuda.current_stream(self.device))
-        # one eager chunk-sized warm call is not needed: the launcher's
-        # occupancy query happens outside capture on first use
-        _ = native.lib()
-        g = torch.cuda.CUDAGraph()
-        with torch.cuda.stream(s):
-            run._warm_params(chunk)
-        with torch.cuda.graph(g, stream=s):
-            run.launch_chunk(chunk)
-        torch.cuda.current_stream(self.device).wait_stream(s)
-        # capturing does not execute: the chunk counter is still at its base
-        return g
+        return run.capture(chunk)
 
 
 def _select_columns(ptr: torch.Tensor, rows: torch.Tensor, w: torch.Tensor, active: np.ndarray):

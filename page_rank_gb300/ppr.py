@@ -210,16 +210,35 @@ class PprRun:
                                        self._step_params(i), self.ws.data_ptr(), self._ws_bytes, st))
         native.check(L.gl_counter_add(self.chunk_base.data_ptr(), n, st))
 
-    def run(self, chunk: int = 8, x0: torch.Tensor | None = None) -> PprResult:
+    def capture(self, chunk: int):
+        """CUDA graph of one chunk of steps over this run's buffers (the steps
+        read their iteration number from the device counter, so one graph
+        serves every chunk)."""
+        dev = self.device
+        s = torch.cuda.Stream(dev)
+        s.wait_stream(torch.cuda.current_stream(dev))
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            self._warm_params(chunk)
+        with torch.cuda.graph(g, stream=s):
+            self.launch_chunk(chunk)
+        torch.cuda.current_stream(dev).wait_stream(s)
+        return g   # capturing does not execute: the counter is still at its base
+
+    def run(self, chunk: int = 8, x0: torch.Tensor | None = None, use_graph: bool = True) -> PprResult:
         chunk = max(2, chunk + (chunk % 2))
         self.init(x0)
+        graph = self.capture(chunk) if use_graph else None
         history: list[float] = []
         col_iter = np.full(self.K, -1, dtype=np.int64)
         iterations = self.max_iterations
         converged = False
         done = 0
         while done < self.max_iterations:
-            self.launch_chunk(chunk)
+            if graph is not None:
+                graph.replay()
+            else:
+                self.launch_chunk(chunk)
             n = min(chunk, self.max_iterations - done)
             res = self.res_hist[done:done + n].cpu().numpy()  # synchronizes the stream
             finished = False
