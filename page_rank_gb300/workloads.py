@@ -16,7 +16,7 @@ import time
 import numpy as np
 import torch
 
-from . import synth
+from . import native, synth
 from .autotune import autotune
 from .engine import PPREngine
 
@@ -182,3 +182,55 @@ def serving_pass(device, rates=(200.0, 800.0, 3200.0), requests_per_rate: int = 
         srv.stop()
     out["admission_waits"] = srv.admission_waits
     return out
+
+
+def kernels(device, log2n: int = 20, K: int = 64, examples: int = 1 << 20) -> dict:
+    """The other kernel families on the SpMM configuration's graph, timed
+    with CUDA events: a device build (8x8, min 8), eight fused PPR steps over
+    K dense columns, and one forward / backward / Adam round of the
+    warm-start network on ``examples`` rows."""
+    from .graph_link.pbr_registry import get_pbr_gpu_meta
+    from .pbr import build_pbr_device, pbr_from_device_csr
+    from .ppr import PprRun, teleport_from_seed_sets
+    from .warmstart import F_IN, MLP
+
+    g = synth.cluster_rmat_graph(log2n=log2n, cluster=64, mean_degree=16, p_intra=0.7, seed=2, device=device)
+    A = g.A
+    n = A.shape[0]
+    ip = torch.from_numpy(A.indptr.astype(np.int32)).to(device)
+    ix = torch.from_numpy(A.indices.astype(np.int32)).to(device)
+    dv = torch.from_numpy(A.data.astype(np.float32)).to(device)
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize(device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize(device)
+        return e0.elapsed_time(e1) / reps
+
+    build_ms = timed(lambda: build_pbr_device(ip, ix, dv, n, n, 8, 8, 8))
+    pd = pbr_from_device_csr(ip, ix, dv, n, n, 8, 8, 8).to(device)
+    meta = get_pbr_gpu_meta(pd)
+    rng = np.random.default_rng(0)
+    seeds = torch.from_numpy(rng.integers(0, n, K).astype(np.int32)).to(device)
+    tp = teleport_from_seed_sets(torch.arange(K + 1, dtype=torch.int32, device=device), seeds, n, 8)
+    x0 = torch.rand((n, K), device=device)
+    x0 /= x0.sum(dim=0, keepdim=True)
+    run = PprRun(meta, n, n, 8, 8, tp, 0.85, 10_000, 0.0, native.GL_PPR_STOP_PER_COLUMN, None)
+    run.init(x0)
+    step_ms = timed(lambda: run.launch_chunk(8)) / 8
+    mlp = MLP(device, 0)
+    Xf = torch.rand((examples, F_IN), device=device)
+    T = torch.rand(examples, device=device)
+    fwd_ms = timed(lambda: mlp.forward(Xf))
+    bwd_ms = timed(lambda: mlp.gradient(Xf, T))
+    return {"workload": f"kernels: n=2^{log2n} clustered R-MAT ({int(A.nnz)} nonzeros), PBR 8x8 min 8; "
+                        f"PPR steps over {K} dense columns; MLP on {examples} rows",
+            "build_ms": round(build_ms, 3), "ppr_step_ms": round(step_ms, 4),
+            "ppr_step_bytes": int(pd.accounted_blocks() * 20 + pd.compressed_nnz() * 4 + 4 * (n + 1)
+                                  + 8 * pd.remainder_nnz() + 8 * n * K),
+            "mlp_forward_ms": round(fwd_ms, 4), "mlp_backward_ms": round(bwd_ms, 4)}
