@@ -225,7 +225,10 @@ class PprRun:
         torch.cuda.current_stream(dev).wait_stream(s)
         return g   # capturing does not execute: the counter is still at its base
 
-    def run(self, chunk: int = 8, x0: torch.Tensor | None = None, use_graph: bool = True) -> PprResult:
+    def run(self, chunk: int = 8, x0: torch.Tensor | None = None, use_graph: bool = False) -> PprResult:
+        """Iterate until the stop rule holds; ``use_graph`` replays one
+        captured chunk (capturing costs about as much as the launches it
+        saves for one query, so it pays only when a run is long)."""
         chunk = max(2, chunk + (chunk % 2))
         self.init(x0)
         graph = self.capture(chunk) if use_graph else None
