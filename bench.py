@@ -256,15 +256,18 @@ def run_ours(args, rank, world, local_rank):
         x.copy_(xh)
     spmm_host_batches(pd, xs[:2], ys[:2])                 # warm (streams, workspace)
     torch.cuda.synchronize()
-    rounds = max(1, args.e2e_steps // nb_e2e)
+    # one call streams all e2e steps (the 4 host buffer pairs in turn), so
+    # the copy pipeline fills once rather than once per 4 batches
+    steps_e2e = max(nb_e2e, args.e2e_steps)
+    xs_all = [xs[i % nb_e2e] for i in range(steps_e2e)]
+    ys_all = [ys[i % nb_e2e] for i in range(steps_e2e)]
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(rounds):
-        spmm_host_batches(pd, xs, ys)
+    spmm_host_batches(pd, xs_all, ys_all)
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = replica_time(e0.elapsed_time(e1) / (rounds * nb_e2e), world, dev)
+    e2e_ms = replica_time(e0.elapsed_time(e1) / steps_e2e, world, dev)
     e2e_value = replica_throughput(B, world, e2e_ms) / 1e9
     x_host, y_host = xs[0], ys[0]
     # every e2e batch carried X, so each host result must equal the device Y
@@ -296,7 +299,8 @@ def run_ours(args, rank, world, local_rank):
                     "h2d_bytes_per_step": int(x_host.numel() * 4),
                     "d2h_bytes_per_step": int(y_host.numel() * 4),
                     "api": "page_rank_gb300.streaming.spmm_host_batches (pinned host X -> device SpMM -> "
-                           "host Y, 4 batches per call, copies of neighbouring batches overlapped)",
+                           "host Y, one call streaming all steps through 4 host buffer pairs, copies of "
+                           "neighbouring batches overlapped)",
                     "host_result_equals_device_result": bool(e2e_exact)},
             "gpu_launches": args.steps,
             "clocks": clocks,
