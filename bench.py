@@ -37,7 +37,8 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "SpMM HBM GB/s (frac of peak)"
 UNIT = "GB/s"
-WORKLOAD = ("spmm: n=2^20 clustered R-MAT (16384 clusters of 64, out-degree 16, 70% intra, "
+def workload_name(log2n: int = 20) -> str:
+    return (f"spmm: n=2^{log2n} clustered R-MAT ({(1 << log2n) // 64} clusters of 64, out-degree 16, 70% intra, "
             "30% R-MAT .57/.19/.19/.05), X 64 FP32 columns, PBR 8x8 min_nnz 8 + CSR remainder")
 FALLBACK_HBM_GBS = 6800.0
 
@@ -285,7 +286,7 @@ def run_ours(args, rank, world, local_rank):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 5),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded clustered R-MAT graph, X ~ U[0,1))",
-            "config": {"workload": WORKLOAD, "n": n, "features": F, "nnz": int(A.nnz),
+            "config": {"workload": workload_name(args.log2n), "n": n, "features": F, "nnz": int(A.nnz),
                        "blocks": nb, "packed_nnz": packed, "remainder_nnz": rem,
                        "alg_bytes_per_step": B,
                        "l2": "inputs larger than L2: %.0f MB touched per step vs 129 MB L2" % (B / 1e6),
@@ -393,7 +394,7 @@ def run_reference(args, rank, world):
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded clustered R-MAT graph, X ~ U[0,1))",
-        "config": {"workload": WORKLOAD, "n": n, "features": F, "nnz": int(A.nnz),
+        "config": {"workload": workload_name(args.log2n), "n": n, "features": F, "nnz": int(A.nnz),
                    "parallelism": f"{cores} host processes"},
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": "port",
