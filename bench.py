@@ -416,7 +416,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--log2n", type=int, default=20,
                     help="graph size (2**log2n nodes); only for small profiling runs")
-    ap.add_argument("--workload", choices=["spmm", "ppr_small", "ppr_batched", "warmstart", "serving", "kernels"],
+    ap.add_argument("--workload", choices=["spmm", "ppr_small", "ppr_batched", "warmstart", "serving", "kernels",
+                                           "edges"],
                     default="spmm",
                     help="spmm (default, the headline line) or a secondary PPR workload")
     args = ap.parse_args()
@@ -433,7 +434,7 @@ def main():
         dev = torch.device("cuda", local_rank)
         torch.cuda.set_device(dev)
         fn = getattr(workloads, args.workload)
-        default_log2n = {"ppr_batched": 22, "warmstart": 21, "kernels": 20}
+        default_log2n = {"ppr_batched": 22, "warmstart": 21, "kernels": 20, "edges": 20}
         out = fn(dev) if args.workload in ("ppr_small", "serving") else \
             fn(dev, log2n=args.log2n if args.log2n != 20 else default_log2n[args.workload])
         out = {"workload": args.workload, **out}

@@ -86,6 +86,37 @@ typedef struct gl_pbr_matrix {
 } gl_pbr_matrix;
 
 /* ======================================================================== */
+/* Edge list -> transition matrix on the device                             */
+/* Replaces the request path of the reference service between the JSON body
+ * and csr_to_pbr: the COO -> CSR construction of A[target, source] = weight
+ * (Backend/server/app.py:111-131) and normalize_transition_matrix
+ * (graph_link/__init__.py:184-207), except that a dangling column stays
+ * empty and is flagged in `dangling` instead of becoming N values of 1/N.  */
+/* ======================================================================== */
+/* Device workspace (bytes) for gl_edges_to_transition; -1 for sizes above
+ * INT32_MAX - 1. */
+int64_t gl_edges_workspace_bytes(int64_t num_nodes, int64_t num_edges);
+
+/* Edges i with 0 <= source[i], target[i] < num_nodes and a finite weight > 0
+ * are kept (others skipped, as app.py:114-122 does); A[target, source] sums
+ * their FP32-rounded weights, duplicates left to right in input order.  With
+ * normalize != 0 every column is divided by its FP32 sum, computed as scipy's
+ * csc.sum(axis=0) does (first entry + numpy pairwise sum of the rest, rows
+ * increasing); exact-zero products are dropped and dangling[j] (may be NULL)
+ * = 1 for a zero column sum.  Outputs: indptr [num_nodes + 1] int32,
+ * indices / data with room for num_edges entries, *nnz (device int64) the
+ * stored count.  Rows come out sorted by column.  Asynchronous on `stream`.
+ * The result equals the reference's bit for bit whenever scipy's per-row sort
+ * keeps duplicate edges in input order (rows of at most 16 entries, at most
+ * two copies of a pair, or equal weights); otherwise a sum of three or more
+ * duplicates may differ in rounding. */
+int gl_edges_to_transition(int64_t num_nodes, int64_t num_edges, const int32_t* source,
+                           const int32_t* target, const double* weight, int32_t normalize,
+                           int32_t* indptr, int32_t* indices, float* data, uint8_t* dangling,
+                           int64_t* nnz, void* workspace, int64_t workspace_bytes,
+                           cudaStream_t stream);
+
+/* ======================================================================== */
 /* PBR builder on the device                                                */
 /* Replaces csr_to_pbr<index_t, scalar_t> (pbr_matrix/pbr_matrix.cpp:340-477,
  * bound at bindings/bindings.cpp:70-73).  Output is bit-identical to the

@@ -150,6 +150,9 @@ class PprStepParams(_c.Structure):
 _SIGS = {
     "gl_last_error": (_c.c_char_p, []),
     "gl_version": (_c.c_int, []),
+    "gl_edges_workspace_bytes": (_i64, [_i64, _i64]),
+    "gl_edges_to_transition": (_c.c_int, [_i64, _i64, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _i64,
+                                          _vp]),
     "gl_pbr_build_workspace_bytes": (_i64, [_i64, _i64, _i64, _i32, _i32]),
     "gl_pbr_build_count": (_c.c_int, [_vp, _vp, _i32, _i64, _i64, _i64, _i32, _i32, _i32, _vp, _i64,
                                       _c.POINTER(BuildCounts), _vp]),

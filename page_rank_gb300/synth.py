@@ -100,8 +100,10 @@ def rmat_targets(rng, m: int, levels: int, a: float, b: float, c: float) -> tupl
     return src, dst
 
 
-def cluster_rmat_graph(log2n: int = 20, cluster: int = 64, mean_degree: int = 16, p_intra: float = 0.7,
-                       rmat=(0.57, 0.19, 0.19, 0.05), seed: int = 2, device=None) -> Graph:
+def cluster_rmat_edges(log2n: int = 20, cluster: int = 64, mean_degree: int = 16, p_intra: float = 0.7,
+                       rmat=(0.57, 0.19, 0.19, 0.05), seed: int = 2) -> tuple[np.ndarray, np.ndarray]:
+    """(source, target) edge arrays of :func:`cluster_rmat_graph`, duplicates
+    included, in generation order."""
     rng = np.random.default_rng(seed)
     n = 1 << log2n
     m = n * mean_degree
@@ -109,7 +111,13 @@ def cluster_rmat_graph(log2n: int = 20, cluster: int = 64, mean_degree: int = 16
     src_i = rng.integers(0, n, m_intra)
     dst_i = (src_i // cluster) * cluster + rng.integers(0, cluster, m_intra)
     src_r, dst_r = rmat_targets(rng, m - m_intra, log2n, rmat[0], rmat[1], rmat[2])
-    return edges_to_transition(np.concatenate([src_i, src_r]), np.concatenate([dst_i, dst_r]), n,
+    return np.concatenate([src_i, src_r]), np.concatenate([dst_i, dst_r])
+
+
+def cluster_rmat_graph(log2n: int = 20, cluster: int = 64, mean_degree: int = 16, p_intra: float = 0.7,
+                       rmat=(0.57, 0.19, 0.19, 0.05), seed: int = 2, device=None) -> Graph:
+    src, dst = cluster_rmat_edges(log2n, cluster, mean_degree, p_intra, rmat, seed)
+    return edges_to_transition(src, dst, 1 << log2n,
                                f"n=2^{log2n}, clusters of {cluster}, mean out-degree {mean_degree}, "
                                f"{int(p_intra * 100)}% intra-cluster, {100 - int(p_intra * 100)}% "
                                f"R-MAT{tuple(rmat)}, seed={seed}", device=device)

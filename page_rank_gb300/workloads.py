@@ -8,6 +8,9 @@
   the stop threshold bounds the distance to the exact fixed point), converged
   columns retired, CUDA-graph chunks, layout chosen by the autotuner;
   compared with the plain one-query-at-a-time GPU path.
+* ``edges``       — the HTTP request path's edge list -> transition matrix
+  step on the device against the host (scipy) path, and a request served
+  twice (the second reuses the resident graph).
 """
 from __future__ import annotations
 
@@ -234,3 +237,92 @@ def kernels(device, log2n: int = 20, K: int = 64, examples: int = 1 << 20) -> di
             "ppr_step_bytes": int(pd.accounted_blocks() * 20 + pd.compressed_nnz() * 4 + 4 * (n + 1)
                                   + 8 * pd.remainder_nnz() + 8 * n * K),
             "mlp_forward_ms": round(fwd_ms, 4), "mlp_backward_ms": round(bwd_ms, 4)}
+
+
+def edges(device, log2n: int = 20, reps: int = 5, request_nodes: int = 20000) -> dict:
+    """The HTTP request path's matrix step: edge list -> column-normalized
+    transition matrix, on the 2^log2n clustered R-MAT edge list (16 edges per
+    node in generation order, duplicates included, unit weights).
+
+    * ``device_ms``: ``gl_edges_to_transition`` with the edges already in
+      device memory (CUDA events, mean of ``reps``);
+    * ``call_ms``: the Python call from host arrays (upload, workspace, the
+      count read back), wall clock;
+    * ``host_ms``: the same step on the host the way the reference does it
+      (scipy COO -> CSR, then the normalize arithmetic), wall clock, once;
+    * ``identical``: device and host results equal bit for bit;
+    * ``request_first_ms`` / ``request_again_ms``: ``POST /api/ppr``'s body
+      on a ``request_nodes``-node graph of the same class, first call (edge
+      list -> PBR on the device) and a repeat (resident graph reused)."""
+    from .transition import (clear_resident_graphs, device_transition, edge_list_csr, normalize_columns,
+                             solve_edge_list_request)
+
+    src, dst = synth.cluster_rmat_edges(log2n)
+    n, m = 1 << log2n, int(src.size)
+    w = np.ones(m)
+    s_d = torch.from_numpy(src.astype(np.int32)).to(device)
+    t_d = torch.from_numpy(dst.astype(np.int32)).to(device)
+    w_d = torch.from_numpy(w).to(device)
+    L = native.lib()
+    ws_bytes = int(L.gl_edges_workspace_bytes(n, m))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=device)
+    indptr = torch.empty(n + 1, dtype=torch.int32, device=device)
+    indices = torch.empty(m, dtype=torch.int32, device=device)
+    data = torch.empty(m, dtype=torch.float32, device=device)
+    dang = torch.empty(n, dtype=torch.uint8, device=device)
+    nnz = torch.empty(1, dtype=torch.int64, device=device)
+    st = torch.cuda.current_stream(device).cuda_stream
+
+    def launch():
+        native.check(L.gl_edges_to_transition(n, m, s_d.data_ptr(), t_d.data_ptr(), w_d.data_ptr(), 1,
+                                              indptr.data_ptr(), indices.data_ptr(), data.data_ptr(),
+                                              dang.data_ptr(), nnz.data_ptr(), ws.data_ptr(), ws_bytes, st))
+
+    for _ in range(2):
+        launch()
+    torch.cuda.synchronize(device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        launch()
+    e1.record()
+    torch.cuda.synchronize(device)
+    device_ms = e0.elapsed_time(e1) / reps
+
+    device_transition(n, src, dst, w, device)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    ip, ix, dv, dg = device_transition(n, src, dst, w, device)
+    call_ms = (time.perf_counter() - t0) * 1e3
+
+    t0 = time.perf_counter()
+    A_norm, dangling = normalize_columns(edge_list_csr(n, src, dst, w))
+    host_ms = (time.perf_counter() - t0) * 1e3
+    identical = (np.array_equal(ip.cpu().numpy(), A_norm.indptr) and np.array_equal(ix.cpu().numpy(), A_norm.indices)
+                 and np.array_equal(dv.cpu().numpy().view(np.uint32), A_norm.data.view(np.uint32))
+                 and np.array_equal(dg.cpu().numpy(), dangling))
+
+    # request path: a small graph of the same class, twice
+    rs, rd = synth.cluster_rmat_edges(int(np.ceil(np.log2(request_nodes))))
+    keep = (rs < request_nodes) & (rd < request_nodes)
+    rs, rd = rs[keep][: 8 * request_nodes], rd[keep][: 8 * request_nodes]
+    ids = [str(i) for i in range(request_nodes)]
+    index_of = {x: i for i, x in enumerate(ids)}
+    src_ids, dst_ids = [ids[i] for i in rs], [ids[i] for i in rd]
+    ones = [1.0] * len(src_ids)
+    clear_resident_graphs()
+    t0 = time.perf_counter()
+    first = solve_edge_list_request(ids, index_of, src_ids, dst_ids, ones, [0, 1, 2], 0.85, 100, 1e-6)
+    first_ms = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    again = solve_edge_list_request(ids, index_of, src_ids, dst_ids, ones, [0, 1, 2], 0.85, 100, 1e-6)
+    again_ms = (time.perf_counter() - t0) * 1e3
+    clear_resident_graphs()
+    same_ranks = bool(np.array_equal(first["ranks"], again["ranks"]))
+    return {"workload_detail": f"edge list of the n=2^{log2n} clustered R-MAT graph: {m} edges, unit weights; "
+                               f"request graph {request_nodes} nodes / {len(src_ids)} edges",
+            "edges": m, "nnz": int(ix.numel()), "device_ms": round(device_ms, 3),
+            "device_edges_per_s": round(m / device_ms * 1e3, 1), "call_ms": round(call_ms, 2),
+            "host_ms": round(host_ms, 1), "identical": bool(identical),
+            "request_first_ms": round(first_ms, 2), "request_again_ms": round(again_ms, 2),
+            "request_same_ranks": same_ranks}

@@ -51,3 +51,31 @@ def assert_pbr_equal(got: dict, want: dict, ctx: str = ""):
         else:
             assert np.array_equal(a.astype(np.uint64) if k == "block_codes" else a,
                                   b.astype(np.uint64) if k == "block_codes" else b), f"{ctx} {k}: differ"
+
+
+def load_edge_cases():
+    """(name, n, source, target, weight, A, An) from edges_cases.npz: the
+    reference service's matrix A and its normalize_transition_matrix An."""
+    z = np.load(GOLDEN / "edges_cases.npz")
+    out = []
+    for name in z["names"]:
+        name = str(name)
+        n = int(z[f"{name}/n"])
+        A = sp.csr_matrix((z[f"{name}/A_data"], z[f"{name}/A_indices"], z[f"{name}/A_indptr"]), shape=(n, n))
+        An = sp.csr_matrix((z[f"{name}/out_data"], z[f"{name}/out_indices"], z[f"{name}/out_indptr"]),
+                           shape=(n, n))
+        out.append((name, n, z[f"{name}/source"], z[f"{name}/target"], z[f"{name}/weight"], A, An))
+    return out
+
+
+def without_dense_columns(An: sp.csr_matrix, dangling: np.ndarray) -> sp.csr_matrix:
+    """The reference's normalized matrix with its dense 1/N dangling columns
+    removed (what the engine stores; it redistributes that mass in-kernel)."""
+    A = sp.csr_matrix(An, copy=True)
+    A.sort_indices()
+    drop = dangling[A.indices]
+    rows = np.repeat(np.arange(A.shape[0]), np.diff(A.indptr))
+    keep = ~drop
+    out = sp.csr_matrix((A.data[keep], (rows[keep], A.indices[keep])), shape=A.shape)
+    out.sort_indices()
+    return out

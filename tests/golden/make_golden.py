@@ -13,6 +13,13 @@ Writes:
 * ``normalize_cases.npz`` — the reference ``normalize_transition_matrix``
   (``Backend/graph_link/graph_link/__init__.py:184-207``) on graphs with
   dangling nodes;
+* ``edges_cases.npz`` — the reference service's edge list -> matrix step
+  (``Backend/server/app.py:111-131``: edges with unknown endpoints or a
+  non-finite / non-positive weight skipped, ``A[target, source] = weight``
+  in FP32 with duplicates summed by scipy) followed by the reference
+  ``normalize_transition_matrix``, on edge lists with invalid edges,
+  duplicates (equal weights, or at most two copies, or short rows), long
+  columns and empty graphs;
 * ``ppr_nx_cases.npz`` — the NetworkX PPR values the reference's accuracy
   test compares against (``Tests/test_ppr_accuracy.py:14-40``), with the
   column-stochastic matrices they come from, so GPU machines without
@@ -86,6 +93,60 @@ def builder_cases():
     return cases
 
 
+def reference_edge_matrix(n, source, target, weight):
+    """The reference service's step from indexed edges to ``A``
+    (``app.py:111-131``), with -1 standing for an id that is not a node."""
+    rows, cols, data = [], [], []
+    for s, t, w in zip(source, target, weight):
+        if s < 0 or t < 0 or not np.isfinite(w) or w <= 0:
+            continue
+        rows.append(int(t))
+        cols.append(int(s))
+        data.append(float(w))
+    return sp.csr_matrix((np.asarray(data, dtype=np.float32),
+                          (np.asarray(rows, dtype=np.int64), np.asarray(cols, dtype=np.int64))),
+                         shape=(n, n))
+
+
+def edge_cases():
+    """(name, n, source, target, weight) lists whose duplicate sums do not
+    depend on the order scipy's per-row sort leaves them in."""
+    rng = np.random.default_rng(20261204)
+    cases = []
+    n = 60
+    m = 700
+    s, t = rng.integers(-1, n, m), rng.integers(-1, n, m)
+    w = rng.choice([1.0, 1.0, 1.0, 2.0, 0.0, -3.0, np.inf, np.nan], m)
+    cases.append(("invalid_and_equal_weight_dups", n, s, t, w))
+    n = 80
+    pairs = np.unique(rng.integers(0, n, (900, 2)), axis=0)
+    rng.shuffle(pairs)
+    twice = pairs[rng.random(len(pairs)) < 0.4]
+    e = np.concatenate([pairs, twice])
+    perm = rng.permutation(len(e))
+    cases.append(("two_copies_distinct_weights", n, e[perm, 0], e[perm, 1], rng.random(len(e)) * 4 + 1e-3))
+    n = 50
+    s = rng.integers(0, n, 300)
+    t = rng.integers(0, n, 300)
+    t[:40] = 7
+    s[:40] = rng.integers(0, 3, 40)    # row 7: 40 entries over 3 columns...
+    keep = (t != 7) | (np.arange(300) < 12)  # ...cut to 12 so the row stays short
+    cases.append(("short_rows_many_copies", n, s[keep], t[keep], rng.random(keep.sum()) * 3 + 0.5))
+    n = 2000
+    m = 6000
+    s = np.concatenate([np.full(1500, 5), rng.integers(0, n, m)])   # column 5: ~1500 entries
+    t = np.concatenate([rng.permutation(n)[:1500], rng.integers(0, n, m)])
+    key = np.unique(np.stack([s, t], 1), axis=0, return_index=True)[1]
+    key.sort()
+    cases.append(("long_column_pairwise", n, s[key], t[key], rng.random(key.size) * 2 + 0.01))
+    cases.append(("no_edges", 5, np.zeros(0, np.int64), np.zeros(0, np.int64), np.zeros(0)))
+    cases.append(("single_self_loop", 1, np.array([0]), np.array([0]), np.array([2.5])))
+    cases.append(("all_invalid", 4, np.array([0, -1, 2]), np.array([1, 1, -1]), np.array([-1.0, 1.0, 1.0])))
+    cases.append(("tiny_weights", 6, np.array([0, 1, 2, 2]), np.array([1, 2, 3, 4]),
+                  np.array([1e-300, 1e-44, 3.0, 1e-30])))
+    return cases
+
+
 def main():
     core = ref_build.load_reference_core()
     if core is None:
@@ -118,6 +179,23 @@ def main():
         norm[f"c{i}/out_data"] = An.data
     norm["count"] = np.array(3)
     np.savez_compressed(HERE / "normalize_cases.npz", **norm)
+
+    edges = {}
+    names = []
+    for name, n, src, dst, w in edge_cases():
+        A = reference_edge_matrix(n, src, dst, w)
+        An = normalize(A)
+        names.append(name)
+        edges[f"{name}/n"] = np.array(n)
+        edges[f"{name}/source"] = np.asarray(src, np.int64)
+        edges[f"{name}/target"] = np.asarray(dst, np.int64)
+        edges[f"{name}/weight"] = np.asarray(w, np.float64)
+        edges[f"{name}/A_indptr"], edges[f"{name}/A_indices"] = A.indptr, A.indices
+        edges[f"{name}/A_data"] = A.data
+        edges[f"{name}/out_indptr"], edges[f"{name}/out_indices"] = An.indptr, An.indices
+        edges[f"{name}/out_data"] = An.data
+    edges["names"] = np.array(names)
+    np.savez_compressed(HERE / "edges_cases.npz", **edges)
 
     import networkx as nx
     ppr = {}
