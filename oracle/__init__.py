@@ -17,6 +17,10 @@ Contents
   iteration and stop rule (``graph_link/__init__.py:258-267``,
   ``kernels/ppr_kernel.cu:130-168``), the dangling-mass-to-personalization
   update (``kernels/ppr_kernel.cu:57-97``), and a direct sparse solve.
+* ``edges.py`` — the reference service's edge list -> normalized matrix step
+  (``Backend/server/app.py:111-131`` + ``normalize_transition_matrix``),
+  including numpy's pairwise column-sum order; pinned against golden
+  fixtures written by the reference's own code path.
 * ``ref_build.py`` — recipe that compiles the reference's own CPU builder into
   ``oracle/_ref/`` where the reference checkout exists (this container), used
   to pin the restatement and to generate ``tests/golden/``.
