@@ -321,6 +321,29 @@ int gl_ppr_step(const gl_pbr_matrix* A, const gl_teleport* tp,
 int gl_counter_add(int32_t* counter, int32_t delta, cudaStream_t stream);
 
 /* ======================================================================== */
+/* Top-k of PPR columns                                                     */
+/* The reference returns all N ranks and leaves the top-X cut to its        */
+/* frontend (Backend/server/app.py:146-158); this selects the k highest     */
+/* entries of each column on the device, so a caller copies k pairs back.   */
+/* ======================================================================== */
+#define GL_TOPK_MAX 2048
+
+/* Device workspace (bytes) for gl_topk_columns; -1 for k outside [0,
+ * GL_TOPK_MAX] or rows above INT32_MAX. */
+int64_t gl_topk_workspace_bytes(int64_t rows, int64_t num_columns, int32_t k);
+
+/* For each selected column c (columns[c], or c itself when columns is NULL)
+ * of the row-major FP32 matrix X [rows][ld]: its k largest entries, sorted by
+ * value descending and equal values by row ascending, into values [C][k] and
+ * indices [C][k] (row numbers); with rows < k the slots past rows hold -inf
+ * and -1.  Exact and deterministic (radix select on the values' bits; +0.0
+ * ranks above -0.0, a NaN with the sign bit clear above +inf).
+ * Asynchronous on `stream`. */
+int gl_topk_columns(const float* X, int64_t rows, int64_t ld, const int32_t* columns,
+                    int64_t num_columns, int32_t k, float* values, int32_t* indices,
+                    void* workspace, int64_t workspace_bytes, cudaStream_t stream);
+
+/* ======================================================================== */
 /* Learned warm start: 2-layer MLP kernels                                  */
 /* No counterpart in the reference.  f_in inputs (<= GL_MLP_MAX_IN) ->      */
 /* GL_MLP_HIDDEN ReLU units -> 1 output.  W1 [hidden][f_in] and w2 [hidden] */

@@ -29,6 +29,7 @@ ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
               "--expt-relaxed-constexpr", "-I", str(INCLUDE), "-I", str(CSRC)]
 
+GL_TOPK_MAX = 2048
 GL_OK = 0
 GL_ERR_INVALID_ARGUMENT = 1
 GL_ERR_UNSUPPORTED_BLOCK = 2
@@ -172,6 +173,8 @@ _SIGS = {
     "gl_ppr_step": (_c.c_int, [_c.POINTER(PbrMatrixDesc), _c.POINTER(TeleportDesc), _vp, _vp, _i64,
                                _c.POINTER(PprStepParams), _vp, _i64, _vp]),
     "gl_counter_add": (_c.c_int, [_vp, _i32, _vp]),
+    "gl_topk_workspace_bytes": (_i64, [_i64, _i64, _i32]),
+    "gl_topk_columns": (_c.c_int, [_vp, _i64, _i64, _vp, _i64, _i32, _vp, _vp, _vp, _i64, _vp]),
     "gl_mlp_forward": (_c.c_int, [_vp, _i64, _i32, _vp, _vp, _vp, _c.c_float, _vp, _vp]),
     "gl_mlp_backward": (_c.c_int, [_vp, _vp, _i64, _i32, _vp, _vp, _vp, _c.c_float, _vp, _vp, _vp]),
     "gl_mlp_adam": (_c.c_int, [_vp, _vp, _vp, _vp, _i64, _c.c_float, _c.c_float, _c.c_float, _c.c_float,

@@ -35,6 +35,7 @@ import torch
 from . import native
 from .engine import PPREngine, certified_tolerance
 from .ppr import PprRun, teleport_from_seed_sets
+from .topk import topk_columns
 
 
 @dataclass
@@ -44,6 +45,7 @@ class Request:
     alpha: float = 0.85
     tol: float = 1e-6
     max_iterations: int = 1000
+    top_k: int | None = None       # set: only the k best nodes come back (top_values / top_nodes)
     rid: int = 0
     t_submit: float = 0.0
     t_admit: float = 0.0
@@ -51,6 +53,8 @@ class Request:
     iterations: int = 0
     converged: bool = False
     result: torch.Tensor | None = None
+    top_values: np.ndarray | None = None
+    top_nodes: np.ndarray | None = None
     error: BaseException | None = None
     done: threading.Event = field(default_factory=threading.Event)
 
@@ -144,13 +148,26 @@ class _Group:
             return 0
         fin = set(finished)
         keep = [c for c in range(len(self.reqs)) if c not in fin]
+        full = [c for c in finished if self.reqs[c].top_k is None]
+        cut = [c for c in finished if self.reqs[c].top_k is not None]
         with torch.cuda.stream(self.stream):
-            out = X.index_select(1, torch.tensor(finished, device=X.device)).cpu()
+            out = X.index_select(1, torch.tensor(full, device=X.device)).cpu() if full else None
+            tops = {}
+            if cut:
+                kmax = max(self.reqs[c].top_k for c in cut)
+                tv, tr = topk_columns(X, kmax, cut)
+                tv, tr = tv.cpu().numpy(), tr.cpu().numpy()
+                tops = {c: (tv[i], tr[i]) for i, c in enumerate(cut)}
             x_keep = X.index_select(1, torch.tensor(keep, device=X.device)) if keep else None
         now = now_fn()
-        for k, c in enumerate(finished):
+        col_of_full = {c: i for i, c in enumerate(full)}
+        for c in finished:
             r = self.reqs[c]
-            r.result = out[:, k]
+            if c in col_of_full:
+                r.result = out[:, col_of_full[c]]
+            else:
+                tv, tr = tops[c]
+                r.top_values, r.top_nodes = tv[: r.top_k].copy(), tr[: r.top_k].astype(np.int64)
             r.iterations = self.col_iters[c]
             r.t_done = now
             r.done.set()
@@ -221,15 +238,20 @@ class PPRServer:
 
     # -- requests -----------------------------------------------------------------
     def submit(self, graph: str, seeds, alpha: float = 0.85, tol: float = 1e-6,
-               max_iterations: int = 1000) -> Request:
+               max_iterations: int = 1000, top_k: int | None = None) -> Request:
+        """Queue a query; ``top_k`` returns only the k highest-ranked nodes
+        (``Request.top_values`` / ``top_nodes``, selected on the device)
+        instead of the full vector (``Request.result``)."""
         if graph not in self.engines:
             raise KeyError(f"unknown graph {graph!r}")
         seeds = np.asarray(seeds, dtype=np.int64)
         n = self.engines[graph].n
         if seeds.size == 0 or seeds.min() < 0 or seeds.max() >= n:
             raise ValueError("seeds must be a non-empty set of node ids of the graph")
+        if top_k is not None and not 1 <= int(top_k) <= native.GL_TOPK_MAX:
+            raise ValueError(f"top_k must be in [1, {native.GL_TOPK_MAX}]")
         r = Request(graph=graph, seeds=seeds, alpha=float(alpha), tol=float(tol), max_iterations=max_iterations,
-                    rid=next(self._ids), t_submit=time.perf_counter())
+                    top_k=None if top_k is None else int(top_k), rid=next(self._ids), t_submit=time.perf_counter())
         self.queue.put(r)
         return r
 

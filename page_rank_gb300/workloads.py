@@ -191,7 +191,8 @@ def kernels(device, log2n: int = 20, K: int = 64, examples: int = 1 << 20) -> di
     """The other kernel families on the SpMM configuration's graph, timed
     with CUDA events: a device build (8x8, min 8), eight fused PPR steps over
     K dense columns, and one forward / backward / Adam round of the
-    warm-start network on ``examples`` rows."""
+    warm-start network on ``examples`` rows, and the top 100 nodes of each of
+    the K columns (``gl_topk_columns``, six passes over the columns)."""
     from .graph_link.pbr_registry import get_pbr_gpu_meta
     from .pbr import build_pbr_device, pbr_from_device_csr
     from .ppr import PprRun, teleport_from_seed_sets
@@ -226,6 +227,8 @@ def kernels(device, log2n: int = 20, K: int = 64, examples: int = 1 << 20) -> di
     run = PprRun(meta, n, n, 8, 8, tp, 0.85, 10_000, 0.0, native.GL_PPR_STOP_PER_COLUMN, None)
     run.init(x0)
     step_ms = timed(lambda: run.launch_chunk(8)) / 8
+    from .topk import topk_columns
+    topk_ms = timed(lambda: topk_columns(x0, 100))
     mlp = MLP(device, 0)
     Xf = torch.rand((examples, F_IN), device=device)
     T = torch.rand(examples, device=device)
@@ -236,6 +239,7 @@ def kernels(device, log2n: int = 20, K: int = 64, examples: int = 1 << 20) -> di
             "build_ms": round(build_ms, 3), "ppr_step_ms": round(step_ms, 4),
             "ppr_step_bytes": int(pd.accounted_blocks() * 20 + pd.compressed_nnz() * 4 + 4 * (n + 1)
                                   + 8 * pd.remainder_nnz() + 8 * n * K),
+            "topk100_ms": round(topk_ms, 4), "topk_bytes_per_pass": int(4 * n * K),
             "mlp_forward_ms": round(fwd_ms, 4), "mlp_backward_ms": round(bwd_ms, 4)}
 
 

@@ -75,3 +75,28 @@ def test_background_loop_latency(device):
         srv.stop()
     s = latency_summary(reqs)
     assert s["completed"] == 60 and s["p99_ms"] >= s["p50_ms"] > 0
+
+
+def test_top_k_requests(device):
+    """Requests asking for their top nodes get exactly the k best entries of
+    the vector they would have received in full (device selection), mixed
+    in one batch with full-vector requests."""
+    from oracle import topk as ot
+    from page_rank_gb300.serving import PPRServer
+    g = _graphs()["g2"]
+    srv = PPRServer(device=device, max_batch=16, chunk=4)
+    srv.add_graph("g", g.A, dangling=g.dangling, block_size=4)
+    rng = np.random.default_rng(4)
+    pairs = []
+    for i in range(6):
+        seeds = rng.choice(g.n, size=int(rng.integers(1, 9)), replace=False)
+        pairs.append((srv.submit("g", seeds, tol=1e-6), srv.submit("g", seeds, tol=1e-6, top_k=[5, 40, 2048][i % 3])))
+    srv.run_until_idle()
+    for full, cut in pairs:
+        assert full.done.is_set() and cut.done.is_set() and cut.result is None
+        k = cut.top_k
+        wv, wr = ot.topk_columns(full.result.numpy()[:, None], k)
+        assert np.array_equal(cut.top_nodes, wr[0].astype(np.int64))
+        assert np.array_equal(cut.top_values, wv[0])
+    with pytest.raises(ValueError):
+        srv.submit("g", [1], top_k=0)

@@ -80,3 +80,21 @@ def test_synthetic_generators_are_column_stochastic_and_seeded():
 def test_certified_tolerance():
     from page_rank_gb300.engine import certified_tolerance
     assert certified_tolerance(1e-6, 0.85) == pytest.approx(1e-6 * 0.15 / 0.85)
+
+
+def test_topk_oracle_matches_numpy_sort():
+    """The top-k oracle is numpy's descending sort for distinct values and
+    takes the lowest rows among equal values."""
+    from oracle import topk as ot
+    rng = np.random.default_rng(0)
+    X = rng.random((500, 3)).astype(np.float32)
+    v, r = ot.topk_columns(X, 10)
+    for c in range(3):
+        order = np.argsort(-X[:, c], kind="stable")[:10]
+        assert np.array_equal(r[c], order) and np.array_equal(v[c], X[order, c])
+    Z = np.zeros((6, 1), np.float32)
+    Z[4, 0] = 1.0
+    v, r = ot.topk_columns(Z, 3)
+    assert r[0].tolist() == [4, 0, 1]
+    v, r = ot.topk_columns(Z, 8)
+    assert r[0].tolist()[-2:] == [-1, -1] and np.isneginf(v[0, -1])
