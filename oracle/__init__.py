@@ -21,6 +21,8 @@ Contents
   (``Backend/server/app.py:111-131`` + ``normalize_transition_matrix``),
   including numpy's pairwise column-sum order; pinned against golden
   fixtures written by the reference's own code path.
+* ``topk.py`` — the top-k selection ``gl_topk_columns`` promises (numpy
+  lexicographic sort on order-preserving keys).
 * ``ref_build.py`` — recipe that compiles the reference's own CPU builder into
   ``oracle/_ref/`` where the reference checkout exists (this container), used
   to pin the restatement and to generate ``tests/golden/``.
