@@ -459,20 +459,22 @@ __device__ __forceinline__ void accumulate_rows(const StripeArgs<S>& a, S* tile,
             off = a.offsets[kc + lane];
         }
         // per-row bit counts of this lane's block, scanned over the warp
-        RowPack<BR> cnt, incl;
-        cnt.clear();
+        // (ex: entries of each row in earlier blocks of the chunk, packed)
+        RowPack<BR> ex;
+        ex.clear();
 #pragma unroll
-        for (int r = 0; r < BR; ++r) cnt.set(r, __popc((uint32_t)(code >> (r * BC)) & ROWMASK));
+        for (int r = 0; r < BR; ++r) ex.set(r, __popc((uint32_t)(code >> (r * BC)) & ROWMASK));
         uint64_t tot_lane = 0;   // lane r / 4 holds the totals word r / 4 after this
 #pragma unroll
         for (int i = 0; i < RowPack<BR>::W; ++i) {
-            uint64_t v = cnt.w[i];
+            const uint64_t mine = ex.w[i];
+            uint64_t v = mine;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const uint64_t u = __shfl_up_sync(0xffffffffu, v, o);
                 if (lane >= o) v += u;
             }
-            incl.w[i] = v;
+            ex.w[i] = v - mine;
             const uint64_t t = __shfl_sync(0xffffffffu, v, 31);
             if ((lane >> 2) == i) tot_lane = t;
         }
@@ -493,63 +495,77 @@ __device__ __forceinline__ void accumulate_rows(const StripeArgs<S>& a, S* tile,
         __syncwarp();
         const bool fits = total <= kListCap;
         if (fits) {
-            // this lane's block entries into its rows' segments
-            if (code) {
-                int32_t k = off;
+            // Every entry is written once, complete (column, value), with
+            // all lanes busy: the unit's remainder entries flat over
+            // [j0, j1), the block entries as (block, row) pairs, one pair
+            // per lane.  Loads of the first remainder rounds and of the
+            // block values are issued before any of them is stored.
+            const int32_t nrem = last ? j1 - j0 : 0;
+            constexpr int kRemRounds = 2;
+            int32_t rcol[kRemRounds];
+            S rval[kRemRounds];
 #pragma unroll
-                for (int r = 0; r < BR; ++r) {
-                    uint32_t rb = (uint32_t)(code >> (r * BC)) & ROWMASK;
-                    int pos = seg[r] + (int)(incl.get(r) - cnt.get(r));
-                    while (rb) {
-                        const int c = __ffs(rb) - 1;
-                        rb &= rb - 1u;
-                        lst[pos++] = make_index_entry(col0 + c, k++, S(0));
+            for (int h = 0; h < kRemRounds; ++h) {
+                const int q = h * 32 + lane;
+                rcol[h] = q < nrem ? a.rem_col[j0 + q] : 0;
+                rval[h] = q < nrem ? a.rem_val[j0 + q] : S(0);
+            }
+            const int npairs = nb * BR;
+            for (int p0 = 0; p0 < npairs; p0 += 32) {
+                const int p = p0 + lane;
+                const int src = (p / BR) & 31;
+                const int r = p % BR;
+                const uint64_t bcode = __shfl_sync(0xffffffffu, code, src);
+                const int32_t bcol0 = __shfl_sync(0xffffffffu, col0, src);
+                const int32_t boff = __shfl_sync(0xffffffffu, off, src);
+                uint64_t bex = 0;
+#pragma unroll
+                for (int i = 0; i < RowPack<BR>::W; ++i) {
+                    const uint64_t w = __shfl_sync(0xffffffffu, ex.w[i], src);
+                    if ((r >> 2) == i) bex = w;
+                }
+                const uint32_t rb = p < npairs ? (uint32_t)(bcode >> (r * BC)) & ROWMASK : 0u;
+                if (rb) {
+                    const int32_t k0 = boff + __popcll(bcode & ((1ull << (r * BC)) - 1ull));
+                    const int32_t pos0 = seg[r] + (int32_t)((bex >> (16 * (r & 3))) & 0xffffu);
+                    S v[BC];
+                    int q = 0;
+#pragma unroll
+                    for (int c = 0; c < BC; ++c) {
+                        if ((rb >> c) & 1u) {
+                            v[c] = a.bdata[k0 + q];
+                            ++q;
+                        }
+                    }
+                    q = 0;
+#pragma unroll
+                    for (int c = 0; c < BC; ++c) {
+                        if ((rb >> c) & 1u) {
+                            lst[pos0 + q] = make_entry<S>(bcol0 + c, v[c]);
+                            ++q;
+                        }
                     }
                 }
             }
-            __syncwarp();
-            // block values and remainder entries, lane-parallel, every row's
-            // loads issued before the first store (one round trip per 32
-            // entries of the longest row, not one per entry or per row)
-            int32_t longest = 0;
+            if (nrem > 0) {
+                // row of remainder entry i: the rows r >= 1 starting at or
+                // before it (row starts are non-decreasing)
+                auto put = [&](int q, int32_t col, S val) {
+                    const int32_t i = j0 + q;
+                    int r = 0;
 #pragma unroll
-            for (int r = 0; r < BR; ++r) {
-                const int32_t l = blen[r] > (last ? rlen[r] : 0) ? blen[r] : (last ? rlen[r] : 0);
-                longest = l > longest ? l : longest;
+                    for (int r2 = 1; r2 < BR; ++r2) r += rstart[r2] <= i ? 1 : 0;
+                    lst[seg[r] + blen[r] + (i - rstart[r])] = make_entry<S>(col, val);
+                };
+#pragma unroll
+                for (int h = 0; h < kRemRounds; ++h)
+                    if (h * 32 + lane < nrem) put(h * 32 + lane, rcol[h], rval[h]);
+                for (int q = kRemRounds * 32 + lane; q < nrem; q += 32) put(q, a.rem_col[j0 + q], a.rem_val[j0 + q]);
             }
-#ifndef GL_FETCH_ROWS
-#define GL_FETCH_ROWS 4
-#endif
-            constexpr int RG = BR < GL_FETCH_ROWS ? BR : GL_FETCH_ROWS;   // rows whose loads fly together
-            for (int j0 = 0; j0 < longest; j0 += 32) {
-                const int q = j0 + lane;
-#pragma unroll
-                for (int r0 = 0; r0 < BR; r0 += RG) {
-                    S bv[RG], rv[RG];
-                    int32_t rc[RG];
-#pragma unroll
-                    for (int h = 0; h < RG; ++h) {
-                        const int r = r0 + h;
-                        const int32_t rl = last ? rlen[r] : 0;
-                        bv[h] = q < blen[r] ? a.bdata[entry_index(lst[seg[r] + q])] : S(0);
-                        rc[h] = q < rl ? a.rem_col[rstart[r] + q] : 0;
-                        rv[h] = q < rl ? a.rem_val[rstart[r] + q] : S(0);
-                    }
-#pragma unroll
-                    for (int h = 0; h < RG; ++h) {
-                        const int r = r0 + h;
-                        const int32_t sg = seg[r], bl = blen[r];
-                        const int32_t rl = last ? rlen[r] : 0;
-                        if (q < bl) lst[sg + q].val = bv[h];
-                        if (q < rl) lst[sg + bl + q] = make_entry<S>(rc[h], rv[h]);
-                    }
-                }
-            }
-#pragma unroll 1
-            for (int r = 0; r < BR; ++r) {   // row padding
-                const int32_t len = blen[r] + (last ? rlen[r] : 0);
-                const int32_t pad = (len + GR - 1) / GR * GR - len;
-                if (lane < pad) lst[seg[r] + len + lane] = make_entry<S>(0, S(0));
+            if (GR > 1 && lane < BR) {   // row padding: lane r pads row r
+                const int32_t len = blen[lane] + (last ? rlen[lane] : 0);
+                const int32_t b = seg[lane];
+                for (int32_t q = len; q < (len + GR - 1) / GR * GR; ++q) lst[b + q] = make_entry<S>(0, S(0));
             }
             __syncwarp();
             if constexpr (NARROW) {
@@ -572,7 +588,7 @@ __device__ __forceinline__ void accumulate_rows(const StripeArgs<S>& a, S* tile,
             } else {
                 uint32_t rb = (uint32_t)(code >> (r * BC)) & ROWMASK;
                 if (rb) {
-                    int pos = (int)(incl.get_dyn(r) - cnt.get_dyn(r));
+                    int pos = (int)ex.get_dyn(r);
                     int32_t k = off + (r == 0 ? 0 : __popcll(code & ((1ull << (r * BC)) - 1ull)));
                     while (rb) {
                         const int c = __ffs(rb) - 1;
