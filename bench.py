@@ -59,10 +59,11 @@ def measured_peak():
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def profile_traffic(nb_scale_bytes: int):
-    """DRAM bytes per launch from the committed ncu summary of this workload."""
+def profile_traffic(log2n: int, features: int):
+    """DRAM bytes per launch from the committed ncu summary of this workload
+    (captured for n = 2^20 and 64 columns only; None for other sizes)."""
     p = ROOT / "profiles" / "stripe_kernel_spmm_rmat2e20_64cols.md"
-    if not p.is_file():
+    if log2n != 20 or features != 64 or not p.is_file():
         return None
     for line in p.read_text().splitlines():
         if line.startswith("dram_bytes_per_launch:"):
@@ -280,7 +281,7 @@ def run_ours(args, rank, world, local_rank):
     out = None
     if rank == 0:
         peak, peak_kind = measured_peak()
-        traffic = profile_traffic(B)
+        traffic = profile_traffic(args.log2n, F)
         out = {
             "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 5),
