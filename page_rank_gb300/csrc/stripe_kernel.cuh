@@ -781,8 +781,17 @@ stripe_kernel(const StripeArgs<S> a) {
         return (int64_t)__shfl_sync(0xffffffffu, v, 0);
     };
     for (int64_t item = a.sched != nullptr ? next_item(0) : warp_id; item < items; item = next_item(item)) {
-        const int64_t u = item / BT;
-        const int64_t bt = item - u * BT;
+        // power-iteration steps number the items column-tile major, so a
+        // warp's successive items mostly share a tile and its per-column
+        // residual sums are flushed (atomically) a few times per launch, not
+        // at nearly every item; the SpMM keeps a unit's tiles adjacent (the
+        // second decode of a stripe finds its matrix data in L2)
+#ifndef GL_TILE_MAJOR_SPMM
+#define GL_TILE_MAJOR_SPMM 0
+#endif
+        constexpr bool tile_major = PPR || GL_TILE_MAJOR_SPMM;
+        const int64_t u = tile_major ? item % units : item / BT;
+        const int64_t bt = tile_major ? item / units : item - u * BT;
         const int64_t b = bt / a.ntiles;
         const int tile = (int)(bt - b * a.ntiles);
         const int col_base = tile * T + c_lane * V;

@@ -100,7 +100,7 @@ def test_ppr_float64_matrix(device):
     assert np.abs(X.cpu().numpy() - X64).sum() < 1e-8
 
 
-@pytest.mark.parametrize("K", [4, 40])
+@pytest.mark.parametrize("K", [4, 40, 200])
 def test_ppr_per_column_alpha_matches_scalar_runs(K, device):
     """Columns with their own alpha / certified threshold in one fused run
     give bit for bit the vectors of runs where every column has that alpha,

@@ -171,3 +171,25 @@ def test_host_batches_pipeline(device):
     torch.cuda.synchronize()
     for x, y in zip(xs, ys):
         _check(y.numpy(), spmm_csr_fp64(A, x.numpy()))
+
+
+@pytest.mark.parametrize("F", [129, 256, 300, 520])
+@pytest.mark.parametrize("block_size", [4, 8])
+def test_spmm_multi_tile_with_heavy_stripes(F, block_size, device):
+    """Several column tiles per stripe (one decoded list consumed once per
+    tile, or decoded again when a stripe's rows do not fit it) together with
+    heavy stripes cut into pieces: a hub row and a hub column."""
+    rng = np.random.default_rng(5)
+    n = 3000
+    A = random_csr(n, 0.004, seed=11).tolil()
+    A[17, :] = (rng.random(n) < 0.6).astype(np.float32) * rng.random(n).astype(np.float32)
+    A[:, 40] = (rng.random((n, 1)) < 0.3).astype(np.float32)
+    A = sp.csr_matrix(A, dtype=np.float32)
+    A.eliminate_zeros()
+    X = random_x(n, F, seed=3)
+    pbr = _gl().csr_to_pbr(A, block_rows=block_size, block_cols=block_size, min_nnz_per_block=2).to(device)
+    Xd = torch.from_numpy(X).to(device)
+    Y = _gl().pbr_matmul(pbr, Xd).cpu().numpy()
+    _check(Y, spmm_csr_fp64(A, X))
+    Y2 = _gl().pbr_matmul(pbr, Xd).cpu().numpy()   # the workspace is left clean for the next call
+    assert np.array_equal(Y, Y2)
