@@ -40,3 +40,14 @@ def test_workspace_query_is_host_only():
     lib = native.lib()
     assert lib.gl_pbr_build_workspace_bytes(1000, 1000, 5000, 8, 8) > 0
     assert lib.gl_pbr_build_workspace_bytes(-1, 10, 10, 2, 2) < 0
+
+
+def test_edge_and_topk_workspace_queries_are_host_only():
+    lib = native.lib()
+    assert lib.gl_edges_workspace_bytes(1000, 5000) > 0
+    assert lib.gl_edges_workspace_bytes(0, 0) > 0
+    assert lib.gl_edges_workspace_bytes(-1, 10) < 0
+    assert lib.gl_edges_workspace_bytes(10, 1 << 40) < 0
+    assert lib.gl_topk_workspace_bytes(1 << 20, 64, 100) > 0
+    assert lib.gl_topk_workspace_bytes(100, 4, native.GL_TOPK_MAX + 1) < 0
+    assert lib.gl_topk_workspace_bytes(-5, 4, 10) < 0

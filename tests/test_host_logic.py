@@ -98,3 +98,15 @@ def test_topk_oracle_matches_numpy_sort():
     assert r[0].tolist() == [4, 0, 1]
     v, r = ot.topk_columns(Z, 8)
     assert r[0].tolist()[-2:] == [-1, -1] and np.isneginf(v[0, -1])
+
+
+def test_dangling_bitmap_matches_host_packing():
+    """The device-side dangling bitmap of the request path packs bits like
+    the engine's host helper (bit j % 32 of word j // 32)."""
+    from page_rank_gb300.engine import _bitmap_from_mask
+    from page_rank_gb300.transition import dangling_bitmap
+    rng = np.random.default_rng(2)
+    for n in (1, 31, 32, 33, 100, 1000):
+        m = rng.random(n) < 0.5
+        m[-1] = True
+        assert torch.equal(dangling_bitmap(torch.from_numpy(m)), _bitmap_from_mask(m, "cpu"))
