@@ -113,6 +113,8 @@ struct StripeArgs {
     int32_t dang_uniform;
     const double* col_alpha;       // [K] or nullptr: alpha for every column
     const double* col_tol;         // [K] or nullptr: tol for every column
+    int32_t cta_sums;              // 1: per-column sums gathered per CTA in shared memory (2 * K doubles
+                                   //    after the stripe buffers), one global atomic per CTA and column
 };
 
 template <typename S, int V>
@@ -746,6 +748,17 @@ stripe_kernel(const StripeArgs<S> a) {
         }
     }
 
+    // per-CTA column sums (residual, dangling) in shared memory behind the
+    // stripe buffers: warps add their partials there, and the CTA adds one
+    // value per column to the FP64 totals at the end
+    double* const s_sums = reinterpret_cast<double*>(xs_dyn + SM::bytes);
+    if constexpr (PPR) {
+        if (a.cta_sums) {
+            for (int i = threadIdx.x; i < 2 * a.K; i += kStripeThreads) s_sums[i] = 0.0;
+            __syncthreads();
+        }
+    }
+
     int64_t cur_bt = -1;
     int cur_col = 0;
     bool cur_ok = false;
@@ -763,9 +776,10 @@ stripe_kernel(const StripeArgs<S> a) {
 #pragma unroll
                 for (int j = 0; j < V; ++j) {
                     const int col = cur_col + j;
-                    if (res_acc[j] != 0.f) atomicAdd(a.res_hist + (int64_t)t * a.K + col, (double)res_acc[j]);
-                    if (a.dbitmap != nullptr && dang_acc[j] != 0.f)
-                        atomicAdd(a.dang_hist + (int64_t)(t + 1) * a.K + col, (double)dang_acc[j]);
+                    double* rdst = a.cta_sums ? s_sums + col : a.res_hist + (int64_t)t * a.K + col;
+                    double* ddst = a.cta_sums ? s_sums + a.K + col : a.dang_hist + (int64_t)(t + 1) * a.K + col;
+                    if (res_acc[j] != 0.f) atomicAdd(rdst, (double)res_acc[j]);
+                    if (a.dbitmap != nullptr && dang_acc[j] != 0.f) atomicAdd(ddst, (double)dang_acc[j]);
                     res_acc[j] = 0.f;
                     dang_acc[j] = 0.f;
                 }
@@ -957,6 +971,16 @@ stripe_kernel(const StripeArgs<S> a) {
         }
     }
     flush();
+    if constexpr (PPR) {
+        if (a.cta_sums) {
+            __syncthreads();
+            for (int c = threadIdx.x; c < a.K; c += kStripeThreads) {
+                const double r = s_sums[c], d = s_sums[a.K + c];
+                if (r != 0.0) atomicAdd(a.res_hist + (int64_t)t * a.K + c, r);
+                if (a.dbitmap != nullptr && d != 0.0) atomicAdd(a.dang_hist + (int64_t)(t + 1) * a.K + c, d);
+            }
+        }
+    }
     if (a.sched != nullptr && lane == 0) {
         // this warp draws nothing more; the last one to retire resets the
         // scheduler for the next launch (nobody waits on anybody)

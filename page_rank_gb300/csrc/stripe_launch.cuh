@@ -15,12 +15,18 @@ int launch_stripe_shape(const StripeArgs<S>& a0, cudaStream_t stream) {
     const int64_t items = units * a.batch * (int64_t)a.ntiles;
     if (items == 0) return GL_OK;
     auto kern = stripe_kernel<S, BR, BR, V, C, PPR>;
-    constexpr size_t smem = StripeSmem<S, BR, V, C>::bytes;
+    constexpr size_t base = StripeSmem<S, BR, V, C>::bytes;
+    // power-iteration steps with up to kCtaSumCols columns gather their
+    // per-column sums per CTA (2 * K doubles of shared memory)
+    constexpr int64_t kCtaSumCols = 512;
+    a.cta_sums = (PPR && a.K <= kCtaSumCols) ? 1 : 0;
+    const size_t smem = base + (a.cta_sums ? (size_t)(2 * a.K) * sizeof(double) : 0);
     static int occ = 0;
     if (occ == 0) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const size_t most = base + (PPR ? (size_t)(2 * kCtaSumCols) * sizeof(double) : 0);
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
         int o = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, kStripeThreads, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, kStripeThreads, most);
         occ = o > 0 ? o : 1;
     }
     int64_t blocks = ceil_div(items, kStripeWarps);
