@@ -223,8 +223,10 @@ __global__ void __launch_bounds__(kTopkThreads) topk_write_kernel(TopkArgs a) {
     int32_t* cr = a.cand_row + c * a.k;
     walk_unit(a, unit, column_of(a, c), [&](int64_t r, uint32_t key) {
         if (key > T) {
-            ck[gt] = key;
-            cr[gt] = (int32_t)r;
+            if (gt < above_total) {   // always true by the selection; keeps every store in bounds
+                ck[gt] = key;
+                cr[gt] = (int32_t)r;
+            }
             ++gt;
         } else if (key == T) {
             if (eq < ties) {
