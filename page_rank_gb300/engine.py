@@ -29,6 +29,7 @@ import torch
 from . import native
 from .pbr import _ptr, pbr_from_device_csr
 from .ppr import PprRun, dangling_bitmap, teleport_from_seed_sets
+from .trace import nvtx_range
 
 
 def certified_tolerance(tol: float, alpha: float) -> float:
@@ -148,6 +149,12 @@ class PPREngine:
         with ``tol`` (the reference's rule).  ``warm_start`` (a trained
         ``warmstart.WarmStart`` of this engine) supplies the start columns
         when ``x0`` is not given; the fixed point is the same."""
+        with nvtx_range(f"engine.solve K={len(seed_sets)}"):
+            return self._solve(seed_sets, alpha, tol, max_iterations, certified, retire, chunk, x0, use_graphs,
+                               compact_ratio, warm_start)
+
+    def _solve(self, seed_sets, alpha, tol, max_iterations, certified, retire, chunk, x0, use_graphs,
+               compact_ratio, warm_start) -> BatchResult:
         K = len(seed_sets)
         dev = self.device
         t0 = time.perf_counter()   # the solve's time includes the warm start's prediction

@@ -26,6 +26,7 @@ from ..pbr import (DataOrder, PBRMatrix, PBRMatrixInt32Double, PBRMatrixInt32Flo
                    spmm_workspace)
 from ..pbr_io import load_pbr, save_pbr
 from ..ppr import PprRun, dangling_bitmap, teleport_from_seed_sets
+from ..trace import nvtx_range
 from .pbr_registry import clear_pbr_gpu_meta, get_pbr_gpu_meta, set_pbr_gpu_meta
 
 
@@ -62,7 +63,7 @@ def pbr_batched_matmul_cuda(pbr_mat, x: torch.Tensor) -> torch.Tensor:
     x3 = x3.contiguous()
     batch, _, width = x3.shape
     y = torch.empty((batch, pbr_mat.rows, width), dtype=x.dtype, device=x.device)
-    with torch.cuda.device(x.device):
+    with torch.cuda.device(x.device), nvtx_range(f"pbr.spmm F={width}"):
         desc = matrix_desc(meta, pbr_mat.rows, pbr_mat.cols, pbr_mat.block_rows, pbr_mat.block_cols)
         ws = spmm_workspace(meta, desc, batch, width, x.device)
         native.check(native.lib().gl_pbr_spmm(desc, x3.data_ptr() if x3.numel() else None,

@@ -21,6 +21,7 @@ import numpy as np
 import torch
 
 from . import native
+from .trace import nvtx_range
 
 
 class DataOrder(enum.IntEnum):
@@ -64,6 +65,13 @@ def build_pbr_device(indptr: torch.Tensor, indices: torch.Tensor, data: torch.Te
                      rows: int, cols: int, block_rows: int, block_cols: int,
                      min_nnz_per_block: int) -> DeviceBuild:
     """Build PBR arrays from a canonical device CSR with the GPU builder."""
+    with nvtx_range(f"pbr.build {block_rows}x{block_cols}"):
+        return _build_pbr_device(indptr, indices, data, rows, cols, block_rows, block_cols, min_nnz_per_block)
+
+
+def _build_pbr_device(indptr: torch.Tensor, indices: torch.Tensor, data: torch.Tensor,
+                      rows: int, cols: int, block_rows: int, block_cols: int,
+                      min_nnz_per_block: int) -> DeviceBuild:
     dev = indptr.device
     if dev.type != "cuda":
         raise RuntimeError("build_pbr_device needs CSR tensors in CUDA memory")

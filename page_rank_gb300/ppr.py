@@ -17,6 +17,7 @@ import torch
 
 from . import native
 from .pbr import _ptr, matrix_desc
+from .trace import nvtx_range
 
 
 @dataclass
@@ -204,11 +205,12 @@ class PprRun:
         """Launch n (even) steps starting at the device counter, then advance it."""
         L = native.lib()
         st = self._stream()
-        for i in range(n):
-            native.check(L.gl_ppr_step(self._desc, self._tpd, self.bufs[i % 2].data_ptr(),
-                                       self.bufs[(i + 1) % 2].data_ptr(), self.K,
-                                       self._step_params(i), self.ws.data_ptr(), self._ws_bytes, st))
-        native.check(L.gl_counter_add(self.chunk_base.data_ptr(), n, st))
+        with nvtx_range(f"ppr.chunk K={self.K}"):
+            for i in range(n):
+                native.check(L.gl_ppr_step(self._desc, self._tpd, self.bufs[i % 2].data_ptr(),
+                                           self.bufs[(i + 1) % 2].data_ptr(), self.K,
+                                           self._step_params(i), self.ws.data_ptr(), self._ws_bytes, st))
+            native.check(L.gl_counter_add(self.chunk_base.data_ptr(), n, st))
 
     def capture(self, chunk: int):
         """CUDA graph of one chunk of steps over this run's buffers (the steps

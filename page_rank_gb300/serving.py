@@ -36,6 +36,7 @@ from . import native
 from .engine import PPREngine, certified_tolerance
 from .ppr import PprRun, teleport_from_seed_sets
 from .topk import topk_columns
+from .trace import nvtx_range
 
 
 @dataclass
@@ -282,6 +283,10 @@ class PPRServer:
 
     def step(self) -> int:
         """One scheduling round; returns the number of requests finished."""
+        with nvtx_range("serving.round"):
+            return self._step()
+
+    def _step(self) -> int:
         self._admit()
         active = []
         for g in self.groups.values():

@@ -10,6 +10,7 @@ from __future__ import annotations
 import torch
 
 from . import native
+from .trace import nvtx_range
 
 
 def topk_columns(X: torch.Tensor, k: int, columns=None) -> tuple[torch.Tensor, torch.Tensor]:
@@ -42,6 +43,11 @@ def topk_columns(X: torch.Tensor, k: int, columns=None) -> tuple[torch.Tensor, t
     if C == 0 or k == 0:
         return values, rows_out
     L = native.lib()
+    with nvtx_range(f"topk k={k} C={C}"):
+        return _topk(L, X, rows, ld, cols, C, k, values, rows_out, dev)
+
+
+def _topk(L, X, rows, ld, cols, C, k, values, rows_out, dev):
     ws_bytes = int(L.gl_topk_workspace_bytes(rows, C, k))
     ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device=dev)
     native.check(L.gl_topk_columns(X.data_ptr() if X.numel() else None, rows, ld,

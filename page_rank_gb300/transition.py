@@ -24,6 +24,7 @@ import scipy.sparse as sp
 import torch
 
 from . import native
+from .trace import nvtx_range
 
 
 def normalize_columns(A_csr: sp.csr_matrix) -> tuple[sp.csr_matrix, np.ndarray]:
@@ -64,6 +65,11 @@ def device_transition(n: int, source, target, weight, device=None, normalize: bo
     src = torch.where((src64 < 0) | (src64 >= n), -1, src64).to(device=dev, dtype=torch.int32)
     dst = torch.where((dst64 < 0) | (dst64 >= n), -1, dst64).to(device=dev, dtype=torch.int32)
     w = w64.to(device=dev)
+    with nvtx_range(f"edges.transition m={m}"):
+        return _device_transition(n, m, src, dst, w, dev, normalize)
+
+
+def _device_transition(n, m, src, dst, w, dev, normalize):
     L = native.lib()
     ws_bytes = int(L.gl_edges_workspace_bytes(n, m))
     if ws_bytes < 0:
