@@ -170,6 +170,17 @@ int gl_pbr_stripe_index(const int32_t* block_coords, int64_t num_blocks, int64_t
                         int32_t block_rows, int32_t* stripe_block_ptr,
                         int32_t* flag_scratch, cudaStream_t stream);
 
+/* Checks PBR arrays built elsewhere (for example by the reference's host
+ * builder, pbr_matrix.cpp:340-477, or read from a file) before they reach a
+ * kernel: offsets start at 0, end at packed_nnz and step by each code's bit
+ * count; block origins lie on the block grid inside the matrix; no code has
+ * bits past the matrix edge; remainder_indptr is a row pointer array ending
+ * at remainder_nnz with columns in range; stripe_block_ptr (when set)
+ * indexes the blocks stripe by stripe.  Reads only inside the declared
+ * sizes.  flag_scratch: one device int32.  Synchronizes `stream`.
+ * Errors: GL_ERR_INVALID_ARGUMENT naming the first failed property. */
+int gl_pbr_validate(const gl_pbr_matrix* A, int32_t* flag_scratch, cudaStream_t stream);
+
 /* int32 elements of the buffer gl_pbr_schedule_build() needs. */
 int64_t gl_pbr_schedule_elems(const gl_pbr_matrix* A, int32_t piece_work);
 

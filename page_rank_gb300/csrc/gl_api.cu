@@ -1,5 +1,6 @@
 // C ABI: error text, SpMM entry point, stripe index, and the personalized
 // PageRank entry points (teleport index, init, fused step).
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <vector>
@@ -95,6 +96,58 @@ __global__ void stripe_work_kernel(const int32_t* stripe_ptr, const int32_t* off
     const int64_t w = (int64_t)offsets[stripe_ptr[s + 1]] - offsets[stripe_ptr[s]] +
                       (int64_t)rem_ptr[last] - rem_ptr[s * br];
     work[s] = (int32_t)(w < INT32_MAX ? w : INT32_MAX);
+}
+
+// Consistency of PBR arrays that did not come from this library's builder
+// (error bits: 1 offsets / popcounts, 2 block coordinates, 4 bits past the
+// matrix edge, 8 remainder row pointers, 16 remainder columns, 32 stripe
+// pointers).  Only reads inside the arrays' declared sizes.
+__global__ void validate_pbr_kernel(const uint64_t* codes, const int32_t* coords, const int32_t* offsets,
+                                    int64_t nb, int64_t packed, const int32_t* rem_ptr, const int32_t* rem_col,
+                                    int64_t rem, const int32_t* stripe_ptr, int64_t rows, int64_t cols, int br,
+                                    int bc, int32_t* flag) {
+    const int64_t ns = ceil_div(rows, br);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int32_t bad = 0;
+    if (i0 == 0) {
+        if (nb > 0 && (offsets[0] != 0 || offsets[nb] != packed)) bad |= 1;
+        if (nb == 0 && packed != 0) bad |= 1;
+        if (rem_ptr[0] != 0 || rem_ptr[rows] != rem) bad |= 8;
+        if (stripe_ptr && (stripe_ptr[0] != 0 || stripe_ptr[ns] != nb)) bad |= 32;
+    }
+    const uint32_t rowmask = bc >= 32 ? 0xffffffffu : ((1u << bc) - 1u);
+    for (int64_t b = i0; b < nb; b += stride) {
+        const uint64_t code = codes[b];
+        if ((int64_t)offsets[b + 1] - offsets[b] != __popcll(code)) bad |= 1;
+        const int64_t r0 = coords[2 * b], c0 = coords[2 * b + 1];
+        if (r0 < 0 || r0 >= rows || c0 < 0 || c0 >= cols || r0 % br != 0 || c0 % bc != 0) {
+            bad |= 2;
+            continue;
+        }
+        uint32_t colbits = 0;
+        for (int r = 0; r < br; ++r) {
+            const uint32_t rb = (uint32_t)(code >> (r * bc)) & rowmask;
+            if (rb && r0 + r >= rows) bad |= 4;
+            colbits |= rb;
+        }
+        if (br * bc < 64 && (code >> (br * bc)) != 0) bad |= 4;
+        if (colbits && c0 + (31 - __clz(colbits)) >= cols) bad |= 4;
+        if (stripe_ptr) {
+            const int64_t s = r0 / br;
+            if (!(b >= stripe_ptr[s] && b < stripe_ptr[s + 1])) bad |= 32;
+        }
+    }
+    for (int64_t r = i0; r < rows; r += stride)
+        if (rem_ptr[r + 1] < rem_ptr[r]) bad |= 8;
+    for (int64_t j = i0; j < rem; j += stride) {
+        const int32_t c = rem_col[j];
+        if (c < 0 || c >= cols) bad |= 16;
+    }
+    if (stripe_ptr)
+        for (int64_t s = i0; s < ns; s += stride)
+            if (stripe_ptr[s + 1] < stripe_ptr[s]) bad |= 32;
+    if (bad) atomicOr(flag, bad);
 }
 
 __global__ void stripe_index_kernel(const int32_t* coords, int64_t nb, int64_t rows, int br, int64_t ns,
@@ -287,6 +340,37 @@ extern "C" int gl_pbr_stripe_index(const int32_t* block_coords, int64_t num_bloc
     GL_CUDA_TRY(cudaStreamSynchronize(stream));
     GL_REQUIRE(flag == 0, GL_ERR_INVALID_ARGUMENT,
                "PBR blocks must be stored stripe-major with row origins that are multiples of block_rows");
+    return GL_OK;
+}
+
+extern "C" int gl_pbr_validate(const gl_pbr_matrix* A, int32_t* flag_scratch, cudaStream_t stream) {
+    GL_REQUIRE(A != nullptr && flag_scratch != nullptr, GL_ERR_INVALID_ARGUMENT, "NULL argument");
+    GL_REQUIRE(A->rows >= 0 && A->cols >= 0 && A->block_rows >= 1 && A->block_cols >= 1 &&
+                   A->block_rows * A->block_cols <= 64 && A->num_blocks >= 0 && A->packed_nnz >= 0 &&
+                   A->remainder_nnz >= 0,
+               GL_ERR_INVALID_ARGUMENT, "bad sizes in the matrix descriptor");
+    GL_REQUIRE(A->remainder_indptr != nullptr, GL_ERR_INVALID_ARGUMENT, "remainder_indptr is NULL");
+    GL_REQUIRE(A->num_blocks == 0 || (A->block_codes && A->block_coords && A->block_offsets),
+               GL_ERR_INVALID_ARGUMENT, "block arrays are NULL");
+    GL_REQUIRE(A->remainder_nnz == 0 || A->remainder_col_ind, GL_ERR_INVALID_ARGUMENT, "remainder_col_ind is NULL");
+    GL_CUDA_TRY(cudaMemsetAsync(flag_scratch, 0, sizeof(int32_t), stream));
+    const int64_t work = std::max<int64_t>(std::max<int64_t>(A->num_blocks, A->rows), A->remainder_nnz) + 1;
+    const int64_t cap = (int64_t)num_sms() * 8;
+    const int64_t grid = std::min<int64_t>(ceil_div(work, 256), cap);
+    validate_pbr_kernel<<<(unsigned)grid, 256, 0, stream>>>(
+        reinterpret_cast<const uint64_t*>(A->block_codes), A->block_coords, A->block_offsets, A->num_blocks,
+        A->packed_nnz, A->remainder_indptr, A->remainder_col_ind, A->remainder_nnz, A->stripe_block_ptr, A->rows,
+        A->cols, A->block_rows, A->block_cols, flag_scratch);
+    GL_LAUNCH_CHECK("validate_pbr_kernel");
+    int32_t flag = 0;
+    GL_CUDA_TRY(cudaMemcpyAsync(&flag, flag_scratch, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+    GL_CUDA_TRY(cudaStreamSynchronize(stream));
+    GL_REQUIRE(!(flag & 1), GL_ERR_INVALID_ARGUMENT, "PBR block_offsets do not match the block codes' bit counts");
+    GL_REQUIRE(!(flag & 2), GL_ERR_INVALID_ARGUMENT, "PBR block coordinates are off the block grid or the matrix");
+    GL_REQUIRE(!(flag & 4), GL_ERR_INVALID_ARGUMENT, "a PBR block code has bits past the matrix edge");
+    GL_REQUIRE(!(flag & 8), GL_ERR_INVALID_ARGUMENT, "PBR remainder_indptr is not a valid row pointer array");
+    GL_REQUIRE(!(flag & 16), GL_ERR_INVALID_ARGUMENT, "a PBR remainder column index is out of range");
+    GL_REQUIRE(!(flag & 32), GL_ERR_INVALID_ARGUMENT, "stripe_block_ptr does not index the blocks stripe by stripe");
     return GL_OK;
 }
 

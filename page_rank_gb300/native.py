@@ -161,6 +161,7 @@ _SIGS = {
                                      _i64, _c.POINTER(BuildCounts), _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                      _vp, _vp]),
     "gl_pbr_stripe_index": (_c.c_int, [_vp, _i64, _i64, _i32, _vp, _vp, _vp]),
+    "gl_pbr_validate": (_c.c_int, [_c.POINTER(PbrMatrixDesc), _vp, _vp]),
     "gl_pbr_schedule_elems": (_i64, [_c.POINTER(PbrMatrixDesc), _i32]),
     "gl_pbr_schedule_build": (_c.c_int, [_c.POINTER(PbrMatrixDesc), _i32, _vp, _i64, _vp]),
     "gl_pbr_spmm_workspace_bytes": (_i64, [_c.POINTER(PbrMatrixDesc), _i64, _i64]),

@@ -59,6 +59,7 @@ class DeviceBuild:
     rem_vals: torch.Tensor     # [rem] value dtype
     stripe_ptr: torch.Tensor   # [ceil(rows / block_rows) + 1] int32
     counts: dict
+    trusted: bool = True       # False: arrays from outside the builder, checked on .to()
 
 
 def build_pbr_device(indptr: torch.Tensor, indices: torch.Tensor, data: torch.Tensor,
@@ -242,6 +243,8 @@ class PBRMatrix:
                 "rem_vals": b.rem_vals.to(dev),
                 "stripe_ptr": b.stripe_ptr.to(dev),
             }
+            if not b.trusted:   # e.g. read from a file: check before any kernel reads them
+                validate_arrays(meta, self.rows, self.cols, self.block_rows, self.block_cols)
             reg.set_pbr_gpu_meta(new, meta)
         return new
 
@@ -285,6 +288,30 @@ def matrix_desc(meta: dict, rows: int, cols: int, block_rows: int, block_cols: i
                 ) -> native.PbrMatrixDesc:
     """C descriptor for a registered (int32-index) device matrix, including its
     load-balance schedule (built on first use and kept in ``meta``)."""
+    d = _array_desc(meta, rows, cols, block_rows, block_cols)
+    sched = meta.get("schedule")
+    if sched is None and block_rows == block_cols and block_rows in (2, 4, 8) and rows > 0:
+        sched = build_schedule(d, meta["stripe_ptr"].device, int(meta.get("piece_work", 0)))
+        meta["schedule"] = sched
+    if sched is not None:
+        for f in SCHED_FIELDS:
+            setattr(d, f, sched[f])
+    return d
+
+
+def validate_arrays(meta: dict, rows: int, cols: int, block_rows: int, block_cols: int) -> None:
+    """``gl_pbr_validate`` on device PBR arrays that did not come from this
+    library's builder; raises ``ValueError`` naming the first broken
+    property (offsets vs bit counts, coordinates, bits past the edge,
+    remainder pointers / columns, stripe pointers)."""
+    d = _array_desc(meta, rows, cols, block_rows, block_cols)
+    dev = meta["rem_indptr"].device
+    flag = torch.empty(1, dtype=torch.int32, device=dev)
+    with torch.cuda.device(dev):
+        native.check(native.lib().gl_pbr_validate(d, flag.data_ptr(), torch.cuda.current_stream(dev).cuda_stream))
+
+
+def _array_desc(meta: dict, rows: int, cols: int, block_rows: int, block_cols: int) -> native.PbrMatrixDesc:
     d = native.PbrMatrixDesc()
     d.rows, d.cols = rows, cols
     d.block_rows, d.block_cols = block_rows, block_cols
@@ -302,13 +329,6 @@ def matrix_desc(meta: dict, rows: int, cols: int, block_rows: int, block_cols: i
     d.stripe_block_ptr = _ptr(meta["stripe_ptr"])
     d.column_tile = int(meta.get("column_tile", 0))
     d.lane_split = int(meta.get("lane_split", 0))
-    sched = meta.get("schedule")
-    if sched is None and block_rows == block_cols and block_rows in (2, 4, 8) and rows > 0:
-        sched = build_schedule(d, meta["stripe_ptr"].device, int(meta.get("piece_work", 0)))
-        meta["schedule"] = sched
-    if sched is not None:
-        for f in SCHED_FIELDS:
-            setattr(d, f, sched[f])
     return d
 
 

@@ -150,7 +150,8 @@ def load_pbr(path, device=None):
     """Read a PBR file into a PBRMatrix whose arrays live on ``device``
     (default: the current CUDA device); call ``.to('cuda')`` as for a built
     matrix.  The blocks must be stored stripe-major, as every builder emits
-    them (checked on the device)."""
+    them (checked on the device); ``.to('cuda')`` also runs the device
+    consistency check (``gl_pbr_validate``) before any kernel reads them."""
     from .pbr import _CLASS_OF, DeviceBuild, stripe_index
 
     meta, a = read_pbr_arrays(path)
@@ -166,6 +167,7 @@ def load_pbr(path, device=None):
         rem_vals=t["remainder_data"].to(dev),
         stripe_ptr=stripe_index(coords.to(torch.int32), meta["rows"], meta["block_rows"]),
         counts={"num_blocks": int(a["block_codes"].size), "packed_nnz": int(a["block_data"].size),
-                "remainder_nnz": int(a["remainder_col_ind"].size)})
+                "remainder_nnz": int(a["remainder_col_ind"].size)},
+        trusted=False)
     cls = _CLASS_OF[(itype, vtype)]
     return cls(meta["rows"], meta["cols"], meta["block_rows"], meta["block_cols"], meta["total_nnz"], build)

@@ -22,6 +22,7 @@ class _Pbr(ctypes.Structure):
                [(n, _P) for n in ("heavy_of", "heavy_stripe", "heavy_first", "piece_heavy")]
 
 _lib.gl_pbr_stripe_index.argtypes = [_P, _I64, _I64, _I32, _P, _P, _P]
+_lib.gl_pbr_validate.argtypes = [ctypes.POINTER(_Pbr), _P, _P]
 _lib.gl_pbr_schedule_elems.argtypes = [ctypes.POINTER(_Pbr), _I32]
 _lib.gl_pbr_schedule_elems.restype = _I64
 _lib.gl_pbr_schedule_build.argtypes = [ctypes.POINTER(_Pbr), _I32, _P, _I64, _P]
@@ -49,6 +50,7 @@ def _descriptor(pbr, meta, dtype, stream):
              meta["data"].numel(), meta["rem_col_ind"].numel(), 0 if dtype == torch.float32 else 1,
              *[ptr(k) for k in ("codes", "coords", "offsets", "data", "rem_indptr", "rem_col_ind",
                                 "rem_vals", "stripe_ptr")])
+    _check(_lib.gl_pbr_validate(ctypes.byref(d), flag.data_ptr(), stream))   # arrays from the host builder
     elems = _lib.gl_pbr_schedule_elems(ctypes.byref(d), 0)
     meta["gb300_sched"] = torch.empty(max(elems, 1), dtype=torch.int32, device=dev)
     _check(_lib.gl_pbr_schedule_build(ctypes.byref(d), 0, meta["gb300_sched"].data_ptr(), elems, stream))
