@@ -460,6 +460,56 @@ __device__ __forceinline__ void accumulate_rows(const StripeArgs<S>& a, S* tile,
             col0 = a.coords[2 * (int64_t)(kc + lane) + 1];
             off = a.offsets[kc + lane];
         }
+        if constexpr (P == 32) {
+            // One column per tile: no list.  Lane b takes block kc + b whole
+            // (its X values, then every stored value in row-major bit order
+            // into one accumulator per block row), the chunk's remainder
+            // entries are spread over the lanes, and a warp reduction per row
+            // leaves the stripe's BR sums in lane 0, which adds them to the
+            // tile (column 0 of each row).
+            S acc[BR];
+#pragma unroll
+            for (int r = 0; r < BR; ++r) acc[r] = S(0);
+            if (lane < nb) {
+                S x[BC];
+#pragma unroll
+                for (int c = 0; c < BC; ++c)
+                    x[c] = (int64_t)col0 + c < a.cols ? Xb[((int64_t)col0 + c) * a.K] : S(0);
+                int32_t k = off;
+#pragma unroll
+                for (int r = 0; r < BR; ++r) {
+#pragma unroll
+                    for (int c = 0; c < BC; ++c) {
+                        if ((code >> (r * BC + c)) & 1ull) {
+                            acc[r] = fma(a.bdata[k], x[c], acc[r]);
+                            ++k;
+                        }
+                    }
+                }
+            }
+            if (last) {
+                for (int32_t i = j0 + lane; i < j1; i += 32) {
+                    int r = 0;
+#pragma unroll
+                    for (int r2 = 1; r2 < BR; ++r2) r += rstart[r2] <= i ? 1 : 0;
+                    const S v = a.rem_val[i] * Xb[(int64_t)a.rem_col[i] * a.K];
+#pragma unroll
+                    for (int r2 = 0; r2 < BR; ++r2) acc[r2] += r2 == r ? v : S(0);
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < BR; ++r) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+            }
+            if (own) {
+#pragma unroll
+                for (int r = 0; r < BR; ++r) tile[r * T] += acc[r];
+            }
+            __syncwarp();
+            if (kc >= b1) break;
+            continue;
+        }
         // per-row bit counts of this lane's block, scanned over the warp
         // (ex: entries of each row in earlier blocks of the chunk, packed)
         RowPack<BR> ex;
