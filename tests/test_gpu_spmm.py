@@ -66,7 +66,7 @@ def test_spmm_batched_3d_and_ragged_rows(block_size, device):
     _check(Y, spmm_csr_fp64(A, X))
 
 
-@pytest.mark.parametrize("F", [1, 20, 64, 100])
+@pytest.mark.parametrize("F", [1, 3, 16, 20, 64, 100])
 def test_spmm_float64(F, device):
     A = random_csr(300, 0.05, dtype=np.float64)
     X = np.random.default_rng(1).random((300, F))
@@ -173,7 +173,7 @@ def test_host_batches_pipeline(device):
         _check(y.numpy(), spmm_csr_fp64(A, x.numpy()))
 
 
-@pytest.mark.parametrize("F", [129, 256, 300, 520])
+@pytest.mark.parametrize("F", [1, 129, 256, 300, 520])
 @pytest.mark.parametrize("block_size", [4, 8])
 def test_spmm_multi_tile_with_heavy_stripes(F, block_size, device):
     """Several column tiles per stripe (one decoded list consumed once per
@@ -193,3 +193,19 @@ def test_spmm_multi_tile_with_heavy_stripes(F, block_size, device):
     _check(Y, spmm_csr_fp64(A, X))
     Y2 = _gl().pbr_matmul(pbr, Xd).cpu().numpy()   # the workspace is left clean for the next call
     assert np.array_equal(Y, Y2)
+
+
+@pytest.mark.parametrize("F", [2, 5, 16])
+def test_spmm_float64_heavy_stripes_one_column_tiles(F, device):
+    """FP64 with fewer than 17 columns runs one column per tile (list-free
+    path, X read with the row stride F) including heavy stripes."""
+    rng = np.random.default_rng(8)
+    n = 2500
+    A = random_csr(n, 0.004, dtype=np.float64, seed=4).tolil()
+    A[9, :] = (rng.random(n) < 0.5) * rng.random(n)
+    A = sp.csr_matrix(A, dtype=np.float64)
+    A.eliminate_zeros()
+    X = rng.random((n, F))
+    pbr = _gl().csr_to_pbr(A, block_rows=8, block_cols=8, min_nnz_per_block=2).to(device)
+    Y = _gl().pbr_matmul(pbr, torch.from_numpy(X).to(device)).cpu().numpy()
+    assert np.allclose(Y, spmm_csr_fp64(A, X), rtol=1e-12, atol=1e-12)
