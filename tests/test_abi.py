@@ -51,3 +51,37 @@ def test_edge_and_topk_workspace_queries_are_host_only():
     assert lib.gl_topk_workspace_bytes(1 << 20, 64, 100) > 0
     assert lib.gl_topk_workspace_bytes(100, 4, native.GL_TOPK_MAX + 1) < 0
     assert lib.gl_topk_workspace_bytes(-5, 4, 10) < 0
+
+
+def _desc(block, rows=16):
+    d = native.PbrMatrixDesc()
+    d.rows, d.cols = rows, rows
+    d.block_rows = d.block_cols = block
+    d.value_type = native.GL_F32
+    return d
+
+
+def test_argument_errors_need_no_gpu():
+    """Argument checks run before any CUDA call, return the documented status
+    and the reference's message, and map to ValueError."""
+    import ctypes
+
+    import pytest
+    lib = native.lib()
+    rc = lib.gl_pbr_spmm(_desc(3), None, None, 1, 4, None, 0, None)
+    assert rc == native.GL_ERR_UNSUPPORTED_BLOCK
+    assert lib.gl_last_error().decode() == ("Unsupported block size for PBR SpMM. "
+                                            "Only 2x2, 4x4, and 8x8 are supported.")   # pbr_kernel.cu:392
+    with pytest.raises(ValueError):
+        native.check(rc)
+    assert lib.gl_pbr_spmm_static(_desc(5), None, None, 1, 4, None) == native.GL_ERR_UNSUPPORTED_BLOCK
+    assert lib.gl_pbr_spmm(None, None, None, 1, 4, None, 0, None) == native.GL_ERR_INVALID_ARGUMENT
+    assert lib.gl_pbr_spmm(_desc(4), None, None, 1, -1, None, 0, None) == native.GL_ERR_INVALID_ARGUMENT
+    assert lib.gl_pbr_spmm(_desc(4, rows=0), None, None, 1, 4, None, 0, None) == native.GL_OK   # nothing to do
+    assert lib.gl_pbr_validate(None, None, None) == native.GL_ERR_INVALID_ARGUMENT
+    nnz = ctypes.c_int64(0)
+    assert lib.gl_edges_to_transition(-1, 0, None, None, None, 1, None, None, None, None,
+                                      ctypes.addressof(nnz), None, 0, None) == native.GL_ERR_INVALID_ARGUMENT
+    assert lib.gl_topk_columns(None, 10, 4, None, 4, native.GL_TOPK_MAX + 1, None, None, None, 0,
+                               None) == native.GL_ERR_INVALID_ARGUMENT
+    assert lib.gl_topk_columns(None, 10, 4, None, 0, 5, None, None, None, 0, None) == native.GL_OK
