@@ -13,6 +13,13 @@ Metric: algorithmic HBM bytes of one SpMM / time, in GB/s:
 (code 8 + coords 8 + offset 4 per block; value 4 per packed entry; remainder
 indptr 4 per row, column 4 + value 4 per entry; X read once, Y written once).
 
+The same line carries ``parity`` (the device build of the timed matrix
+against the CPU restatement of the reference builder, and the timed Y against
+the FP64 product) and ``ppr``: the second half of the metric, queries/s of
+batched, one-query-at-a-time and warm-started PPR on the 2**22-node
+cluster / Zipf graph (256 seed sets of 1-32 seeds, L1 1e-6), their FP64
+distance on sampled columns, and an FP64 CPU PPR baseline on all host cores.
+
 Usage:
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 Under torchrun (N > 1) every rank runs an independent replica on its own GPU
@@ -276,6 +283,7 @@ def run_ours(args, rank, world, local_rank):
     # of the timed loop bit for bit (the kernel is deterministic)
     y_dev = Y.cpu()
     e2e_exact = all(torch.equal(y, y_dev) for y in ys)
+    ys = xs = xs_all = ys_all = None
     clocks = sampler.summary(t0, t1)
 
     out = None
@@ -312,8 +320,232 @@ def run_ours(args, rank, world, local_rank):
             gbs, reps, dt = cpu_spmm_rate(A, Xn, B, budget_s=args.cpu_budget)
             out["cpu_baseline"] = {"value": round(gbs, 3), "unit": UNIT, "cores": 1, "kind": "port",
                                    "sample": f"full SpMM (scipy FP32 CSR @ X, the reference's CPU "
-                                             f"check), {reps} reps, {dt * 1e3:.1f} ms each"}
+                                             f"check), {reps} reps, {dt * 1e3:.1f} ms each",
+                                   "cpu": host_cpu()}
+            out["parity"] = cpu_spmm_checks(A, pbr, Xn, y_dev.numpy())
+    if rank == 0 and world == 1 and not args.no_ppr:
+        del X, Y, ws, pd, pbr, A
+        torch.cuda.empty_cache()
+        out["ppr"] = run_ppr(dev, args)
     return out
+
+
+def host_cpu() -> dict:
+    """Host core count and CPU model (lscpu), reported beside CPU numbers."""
+    model = None
+    try:
+        txt = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in txt.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"nproc": os.cpu_count(), "model": model}
+
+
+def cpu_spmm_checks(A, pbr, X: np.ndarray, Y: np.ndarray) -> dict:
+    """CPU side of the SpMM line: the CPU restatement of the reference builder
+    (pbr_matrix.cpp:340-477) timed on the same matrix and compared array by
+    array with the device build that was timed, and the timed Y against the
+    FP64 product (row-split over the host cores)."""
+    import oracle
+    from oracle.ppr import RowSplitMatrix
+
+    n = A.shape[0]
+    t0 = time.perf_counter()
+    o = oracle.csr_to_pbr(A.indptr, A.indices, A.data, n, n, 8, 8, 8)
+    build_s = time.perf_counter() - t0
+    exact = True
+    for k in ("block_codes", "block_coords", "block_offsets", "block_data",
+              "remainder_indptr", "remainder_col_ind", "remainder_data"):
+        a, b = np.asarray(getattr(pbr, k)), np.asarray(o[k])
+        exact &= a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8))
+    M = RowSplitMatrix(A.astype(np.float64))
+    try:
+        Yref = M @ X.astype(np.float64)
+    finally:
+        M.close()
+    rel = np.abs(Y.astype(np.float64) - Yref) / np.maximum(np.abs(Yref), 1e-30)
+    return {"build_exact": bool(exact), "cpu_build_s": round(build_s, 2),
+            "cpu_build": "single-threaded CPU restatement of the reference builder",
+            "spmm_max_rel": float(rel.max()), "spmm_tol": 1e-5,
+            "spmm_reference": "FP64 scipy CSR product of the same matrix and X"}
+
+
+# ---------------------------------------------------------------------------
+# PPR queries/s: the second half of the metric
+PPR_ALPHA = 0.85
+PPR_TOL = 1e-6
+
+
+def run_ppr(dev, args) -> dict:
+    """Batched vs one-query-at-a-time vs warm-started PPR on the 2**22-node
+    cluster / Zipf graph (mean distinct out-degree 20, 80% of each node's
+    edges inside its 64-node cluster), 256 seed sets of 1-32 uniform seeds,
+    alpha 0.85, per-column certified L1 1e-6, converged columns retired,
+    CUDA-graph chunks, layout from the autotuner.  Graph generation, the
+    autotuner and the warm start's training run before the timed solves and
+    are reported in seconds.  The CPU leg solves a sample of the same queries
+    with the FP64 power iteration on all host cores; its vectors are the
+    references the GPU columns are compared with."""
+    import torch
+
+    from page_rank_gb300 import synth
+    from page_rank_gb300.autotune import autotune
+    from page_rank_gb300.engine import PPREngine
+    from page_rank_gb300.warmstart import WarmStart
+
+    K = 256
+    t0 = time.perf_counter()
+    g = synth.cluster_zipf_graph(log2n=args.ppr_log2n, mean_degree=20.0, seed=3, device=dev)
+    gen_s = time.perf_counter() - t0
+    sets = synth.seed_sets(g.n, K, 1, 32, seed=11)
+    t0 = time.perf_counter()
+    tuned = autotune(g.A, K, device=dev)
+    tune_s = time.perf_counter() - t0
+    eng = PPREngine(g.A, block_size=tuned.block_size, min_nnz_per_block=tuned.min_nnz, device=dev,
+                    dangling=g.dangling, column_tile=tuned.column_tile)
+    eng.solve(sets, alpha=PPR_ALPHA, tol=PPR_TOL)           # every launch shape and workspace once
+    torch.cuda.synchronize(dev)
+    sampler = ClockSampler(dev.index or 0)
+    sampler.start()
+    c0 = time.time()
+    rb = eng.solve(sets, alpha=PPR_ALPHA, tol=PPR_TOL, retire=True, use_graphs=True)
+    c1 = time.time()
+    clocks = sampler.summary(c0, c1)
+    plain_n = 16
+    eng.solve_plain(sets[:2], alpha=PPR_ALPHA, tol=PPR_TOL)
+    rp = eng.solve_plain(sets[:plain_n], alpha=PPR_ALPHA, tol=PPR_TOL)
+    sampler.stop()
+    # warm start: the network trained on plain-method vectors of this graph
+    ws = WarmStart(eng, seed=0)
+    t0 = time.perf_counter()
+    stats = ws.train(num_vectors=args.ppr_train_vectors, batch=256, nodes_per_vector=512, epochs=3)
+    train_s = time.perf_counter() - t0
+    ws.solve(sets[:8], alpha=PPR_ALPHA, tol=PPR_TOL)
+    torch.cuda.synchronize(dev)
+    rw = ws.solve(sets, alpha=PPR_ALPHA, tol=PPR_TOL, retire=True, use_graphs=True)
+    qps_b = K / rb.seconds
+    qps_p = plain_n / rp.seconds
+    qps_w = K / rw.seconds
+    same = float((rb.X.double() - rw.X.double()).abs().sum(dim=0).max().item())
+    out = {
+        "workload": f"batched PPR: {g.description}; {K} seed sets of 1-32 uniform seeds, alpha {PPR_ALPHA}, "
+                    f"per-column L1 {PPR_TOL:g} to the fixed point (certified stop), retirement + CUDA graphs",
+        "n": g.n, "nnz": int(g.A.nnz), "graph_gen_s": round(gen_s, 2), "autotune_s": round(tune_s, 2),
+        "layout": {"block": tuned.block_size, "min_nnz": tuned.min_nnz, "column_tile": tuned.column_tile},
+        "batched": {"queries_per_s": round(qps_b, 2), "seconds": round(rb.seconds, 4),
+                    "iterations_sum": int(rb.iterations.sum()), "launched_steps": rb.launched_iterations,
+                    "column_steps": rb.column_steps, "all_converged": bool(rb.converged.all())},
+        "plain": {"queries_per_s": round(qps_p, 2), "sample": plain_n, "seconds": round(rp.seconds, 4),
+                  "iterations_sum": int(rp.iterations.sum())},
+        "batched_warm": {"queries_per_s": round(qps_w, 2), "seconds_including_prediction": round(rw.seconds, 4),
+                         "iterations_sum": int(rw.iterations.sum()), "column_steps": rw.column_steps,
+                         "columns_using_prediction": float(np.mean(rw.warm_columns)),
+                         "train_vectors": stats.vectors, "train_s": round(train_s, 2),
+                         "all_converged": bool(rw.converged.all())},
+        "speedup_batched_vs_plain": round(qps_b / qps_p, 2),
+        "speedup_batched_warm_vs_plain": round(qps_w / qps_p, 2),
+        "iterations_cold_over_warm": round(float(rb.iterations.sum()) / max(1, int(rw.iterations.sum())), 3),
+        "max_l1_cold_vs_warm": same,
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        sample = list(range(min(cores, K)))
+        cpu = cpu_ppr_leg(g, [sets[i] for i in sample], cores)
+        Xg = rb.X[:, torch.tensor(sample, device=dev)].double().cpu().numpy()
+        Xw = rw.X[:, torch.tensor(sample, device=dev)].double().cpu().numpy()
+        d_b = np.abs(Xg - cpu["X"]).sum(axis=0) + cpu["bound"]
+        d_w = np.abs(Xw - cpu["X"]).sum(axis=0) + cpu["bound"]
+        out["parity"] = {"max_l1_vs_fp64": float(d_b.max()), "max_l1_warm_vs_fp64": float(d_w.max()),
+                         "tol": PPR_TOL, "columns": len(sample),
+                         "reference": "FP64 power iteration continued to a certified distance "
+                                      f"< {cpu['bound'].max():.1e} of the exact fixed point"}
+        out["cpu_baseline"] = {"value": round(cpu["qps"], 4), "unit": "queries/s", "cores": cpu["cores"],
+                               "kind": "port", "cpu": host_cpu(),
+                               "sample": f"{len(sample)} of the seed sets, one per process, FP64 scipy power "
+                                         f"iteration (the reference update and stop rule, certified L1 "
+                                         f"{PPR_TOL:g}), {cpu['seconds']:.1f} s wall"}
+        out["speedup_batched_vs_cpu"] = round(qps_b / cpu["qps"], 1)
+    return out
+
+
+def _ppr_worker(args):
+    """One query of the CPU PPR baseline (runs in a spawned process): FP64
+    power iteration x <- alpha A x + (1 - alpha) v, timed to the certified
+    stop, then continued (untimed) to a tight reference."""
+    from multiprocessing import shared_memory
+
+    import scipy.sparse as sp
+
+    names, shapes, dtypes, n, seeds, alpha, thr, ref_bound, q = args
+    shms = [shared_memory.SharedMemory(name=nm) for nm in names]
+    try:
+        indptr, indices, data, out = [np.ndarray(s, dtype=d, buffer=m.buf) for m, s, d in zip(shms, shapes, dtypes)]
+        A = sp.csr_matrix((data, indices, indptr), shape=(n, n))
+        v = np.zeros(n)
+        v[np.asarray(seeds, dtype=np.int64)] = 1.0 / len(seeds)
+        x = v.copy()
+        t0 = time.perf_counter()
+        dt = None
+        cert = np.inf
+        for _ in range(100000):
+            xn = alpha * (A @ x) + (1.0 - alpha) * v
+            upd = float(np.abs(xn - x).sum())
+            x = xn
+            if dt is None and upd < thr:
+                dt = time.perf_counter() - t0
+            cert = alpha / (1.0 - alpha) * upd
+            if cert < ref_bound:
+                break
+        out[:, q] = x
+        return dt, cert
+    finally:
+        for m in shms:
+            m.close()
+
+
+def cpu_ppr_leg(g, seed_sets, cores: int) -> dict:
+    """FP64 power iteration for each seed set, one per spawned process (all
+    host cores): queries/s to the certified L1 stop, and the FP64 vectors
+    continued to a certified distance below 1e-10 of the fixed point."""
+    import multiprocessing as mp
+    from multiprocessing import shared_memory
+
+    assert not np.any(g.dangling), "the CPU leg covers graphs without dangling nodes"
+    n = g.n
+    A = g.A
+    arrays = [A.indptr.astype(np.int32), A.indices.astype(np.int32), A.data.astype(np.float64),
+              np.zeros((n, len(seed_sets)), np.float64)]
+    shms, names = [], []
+    for a in arrays:
+        m = shared_memory.SharedMemory(create=True, size=max(1, a.nbytes))
+        np.ndarray(a.shape, dtype=a.dtype, buffer=m.buf)[...] = a
+        shms.append(m)
+        names.append(m.name)
+    shapes = [a.shape for a in arrays]
+    dtypes = [a.dtype for a in arrays]
+    thr = PPR_TOL * (1.0 - PPR_ALPHA) / PPR_ALPHA
+    jobs = [(names, shapes, dtypes, n, list(map(int, s)), PPR_ALPHA, thr, 1e-10, q)
+            for q, s in enumerate(seed_sets)]
+    try:
+        with mp.get_context("spawn").Pool(min(cores, len(jobs))) as pool:
+            t0 = time.perf_counter()
+            res = pool.map(_ppr_worker, jobs)
+            wall = time.perf_counter() - t0
+        X = np.ndarray(shapes[3], dtype=dtypes[3], buffer=shms[3].buf).copy()
+    finally:
+        for m in shms:
+            m.close()
+            m.unlink()
+    times = np.array([r[0] for r in res], dtype=np.float64)
+    # all queries ran concurrently: the slowest one's time to its stop bounds
+    # the batch's wall time
+    span = float(times.max())
+    return {"qps": len(seed_sets) / span, "seconds": span, "cores": min(cores, len(jobs)), "X": X,
+            "bound": np.array([r[1] for r in res]), "total_wall_s": wall}
 
 
 # ---------------------------------------------------------------------------
@@ -414,6 +646,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ppr", action="store_true", help="skip the PPR queries/s part of the line")
+    ap.add_argument("--ppr-log2n", type=int, default=22)
+    ap.add_argument("--ppr-train-vectors", type=int, default=2048)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--log2n", type=int, default=20,
                     help="graph size (2**log2n nodes); only for small profiling runs")

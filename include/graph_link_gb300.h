@@ -83,6 +83,10 @@ typedef struct gl_pbr_matrix {
     const int32_t* heavy_stripe;        /* [num_heavy]                       */
     const int32_t* heavy_first;         /* [num_heavy + 1]: first piece      */
     const int32_t* piece_heavy;         /* [num_pieces]: owning heavy index  */
+    /* SpMM kernel: 0 automatic, 1 the stripe kernel, 2 the window kernel
+     * (see gl_pbr_spmm; falls back to the stripe kernel where it does not
+     * apply).  Added in ABI version 101. */
+    int32_t kernel;
 } gl_pbr_matrix;
 
 /* ======================================================================== */
@@ -199,7 +203,16 @@ int gl_pbr_schedule_build(gl_pbr_matrix* A, int32_t piece_work, int32_t* buffer,
 /* ======================================================================== */
 /* X: [batch][cols][features], Y: [batch][rows][features], both contiguous,
  * element type A->value_type.  Supported blocks: 2x2, 4x4, 8x8 (others give
- * GL_ERR_UNSUPPORTED_BLOCK, as the reference throws std::invalid_argument). */
+ * GL_ERR_UNSUPPORTED_BLOCK, as the reference throws std::invalid_argument).
+ *
+ * Two kernels implement it.  The window kernel (FP32, features % 4 == 0 and
+ * >= 64, 16-byte aligned X and Y, a workspace, a schedule built with
+ * piece_work <= 256, cols < 2^29) stages the 64 X rows of each 64-row window
+ * in shared memory with bulk asynchronous copies and reads the nonzeros of
+ * the window's diagonal block from there; every other case runs the stripe
+ * kernel.  A->kernel selects one explicitly.  The window kernel records a
+ * bounded wait that gave up, or a unit too large for its lists, in the
+ * workspace (gl_spmm_workspace_error). */
 /* Workspace (bytes) of gl_pbr_spmm / gl_ppr_step for A's schedule: partial
  * tiles of the heavy-stripe pieces plus one counter per heavy stripe and
  * tile.  It must be zero-filled before its first use; every call leaves the
@@ -209,6 +222,13 @@ int64_t gl_pbr_spmm_workspace_bytes(const gl_pbr_matrix* A, int64_t batch, int64
 int gl_pbr_spmm(const gl_pbr_matrix* A, const void* X, void* Y,
                 int64_t batch, int64_t features, void* workspace, int64_t workspace_bytes,
                 cudaStream_t stream);
+
+/* Reads and clears the error word a window-kernel launch leaves in its
+ * workspace: GL_OK, GL_ERR_TIMEOUT (a bounded wait gave up) or
+ * GL_ERR_INVALID_ARGUMENT (a unit had more entries than its list; the
+ * schedule did not match the matrix).  Synchronizes `stream`.  No
+ * counterpart in the reference. */
+int gl_spmm_workspace_error(void* workspace, cudaStream_t stream);
 
 /* gl_pbr_spmm for callers that cannot allocate device memory when they call
  * it (a host program whose device memory is all owned by its own allocator,

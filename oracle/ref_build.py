@@ -25,6 +25,9 @@ exists; the GPU machines never build it.
 Usage::
 
     python oracle/ref_build.py          # builds oracle/_ref/graph_link_core*.so
+
+The reference checkout is taken from ``$GL_REFERENCE_ROOT`` or, when that is
+unset, from a directory named ``reference`` beside this repository.
 """
 from __future__ import annotations
 
@@ -33,7 +36,16 @@ import os
 import sys
 from pathlib import Path
 
-REFERENCE_ROOT = Path(os.environ.get("GL_REFERENCE_ROOT", "/root/reference"))
+def _reference_root() -> Path:
+    """The reference checkout: $GL_REFERENCE_ROOT, else a directory named
+    ``reference`` beside this repository's directory."""
+    env = os.environ.get("GL_REFERENCE_ROOT")
+    if env:
+        return Path(env)
+    return Path(__file__).resolve().parents[2] / "reference"
+
+
+REFERENCE_ROOT = _reference_root()
 REF_SRC = REFERENCE_ROOT / "Backend" / "graph_link"
 OUT_DIR = Path(__file__).resolve().parent / "_ref"
 

@@ -61,6 +61,7 @@ StripeArgs<S> make_args(const gl_pbr_matrix* A) {
     a.heavy_stripe = A->heavy_stripe;
     a.heavy_first = A->heavy_first;
     a.piece_heavy = A->piece_heavy;
+    a.variant = A->kernel;
     return a;
 }
 
@@ -233,7 +234,7 @@ __global__ void counter_add_kernel(int32_t* c, int32_t d) { *c += d; }
 using namespace gl;
 
 extern "C" const char* gl_last_error(void) { return last_error(); }
-extern "C" int gl_version(void) { return 100; }
+extern "C" int gl_version(void) { return 101; }
 
 extern "C" int64_t gl_pbr_spmm_workspace_bytes(const gl_pbr_matrix* A, int64_t batch, int64_t features) {
     if (A == nullptr || batch < 0 || features < 0) return -1;
@@ -323,6 +324,17 @@ extern "C" int gl_pbr_spmm(const gl_pbr_matrix* A, const void* X, void* Y, int64
     a.Y = static_cast<double*>(Y);
     if ((rc = bind_workspace(a, A, batch, features, workspace, workspace_bytes)) != GL_OK) return rc;
     return launch_stripe<double, false>(a, A->block_rows, A->block_cols, A->column_tile, A->lane_split, stream);
+}
+
+extern "C" int gl_spmm_workspace_error(void* workspace, cudaStream_t stream) {
+    GL_REQUIRE(workspace != nullptr, GL_ERR_INVALID_ARGUMENT, "workspace is NULL");
+    int32_t* word = reinterpret_cast<int32_t*>(static_cast<char*>(workspace) + 16);
+    int32_t v = 0;
+    GL_CUDA_TRY(cudaMemcpyAsync(&v, word, sizeof(v), cudaMemcpyDeviceToHost, stream));
+    GL_CUDA_TRY(cudaMemsetAsync(word, 0, sizeof(v), stream));
+    GL_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (v != GL_OK) set_error("a window-kernel launch on this workspace reported status %d", v);
+    return v;
 }
 
 extern "C" int gl_pbr_stripe_index(const int32_t* block_coords, int64_t num_blocks, int64_t rows, int32_t block_rows,

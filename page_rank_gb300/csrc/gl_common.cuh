@@ -3,7 +3,9 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
+#include <mutex>
 #include <cstdio>
 #include <string>
 
@@ -39,15 +41,48 @@ inline int cuda_status(cudaError_t e, const char* what) {
         if (!(cond)) { ::gl::set_error(__VA_ARGS__); return (code); }       \
     } while (0)
 
-inline int num_sms() {
-    static int cached = 0;
-    if (cached == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev);
-        if (cached <= 0) cached = 152;
+// Per-device caches: one slot per device index, filled the first time that
+// device asks (under setup_mutex(), with the device current).
+constexpr int kMaxDevices = 64;
+inline std::mutex& setup_mutex() {
+    static std::mutex m;
+    return m;
+}
+
+// Runs init(&value) once per device (it may set function attributes, which
+// are per device, and returns a GL_* status) and caches the positive value
+// it produces in cache[device].
+template <typename Init>
+int per_device_value(std::atomic<int> (&cache)[kMaxDevices], Init init, int* out) {
+    int dev = 0;
+    GL_CUDA_TRY(cudaGetDevice(&dev));
+    GL_REQUIRE(dev >= 0 && dev < kMaxDevices, GL_ERR_INVALID_ARGUMENT, "device index %d out of range", dev);
+    int v = cache[dev].load(std::memory_order_acquire);
+    if (v <= 0) {
+        std::lock_guard<std::mutex> lock(setup_mutex());
+        v = cache[dev].load(std::memory_order_acquire);
+        if (v <= 0) {
+            const int rc = init(&v);
+            if (rc != GL_OK) return rc;
+            if (v <= 0) v = 1;
+            cache[dev].store(v, std::memory_order_release);
+        }
     }
-    return cached;
+    *out = v;
+    return GL_OK;
+}
+
+// SM count of the current device (cached per device).
+inline int num_sms() {
+    static std::atomic<int> cache[kMaxDevices];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return 152;
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (v <= 0) {
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 152;
+        cache[dev].store(v, std::memory_order_relaxed);
+    }
+    return v;
 }
 
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }

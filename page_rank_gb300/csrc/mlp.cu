@@ -216,11 +216,19 @@ extern "C" int gl_mlp_backward(const float* X, const float* target, int64_t n, i
     GL_REQUIRE(grad != nullptr, GL_ERR_INVALID_ARGUMENT, "grad is NULL");
     if (n == 0) return GL_OK;
     const size_t smem = sizeof(float) * (H * FMAX + 2 * H + kChunk * H + kChunk * FMAX + kChunk);
-    static bool attr = false;
-    if (!attr) {
-        GL_CUDA_TRY(cudaFuncSetAttribute(mlp_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr = true;
-    }
+    // the shared-memory attribute is per device: set once on every device
+    static std::atomic<int> attr_cache[kMaxDevices];
+    int attr = 0;
+    rc = per_device_value(
+        attr_cache,
+        [&](int* v) {
+            GL_CUDA_TRY(
+                cudaFuncSetAttribute(mlp_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            *v = 1;
+            return GL_OK;
+        },
+        &attr);
+    if (rc != GL_OK) return rc;
     int64_t blocks = ceil_div(n, kChunk);
     const int64_t cap = (int64_t)num_sms() * 2;
     if (blocks > cap) blocks = cap;

@@ -35,8 +35,6 @@ namespace {
 
 static __device__ __align__(256) unsigned char g_spmm_scratch[GL_SPMM_STATIC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
 void* g_scratch_addr[kMaxDevices] = {};
 
 // Device address of g_spmm_scratch on the current device (set up once per
@@ -46,7 +44,7 @@ int scratch_address(void** out) {
     int dev = 0;
     GL_CUDA_TRY(cudaGetDevice(&dev));
     GL_REQUIRE(dev >= 0 && dev < kMaxDevices, GL_ERR_INVALID_ARGUMENT, "device index %d out of range", dev);
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    std::lock_guard<std::mutex> lock(setup_mutex());
     if (g_scratch_addr[dev] == nullptr) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_spmm_scratch);
@@ -82,6 +80,7 @@ StripeArgs<S> static_args(const gl_pbr_matrix* A, const void* X, void* Y, int64_
     a.heavy_stripe = A->heavy_stripe;
     a.heavy_first = A->heavy_first;
     a.piece_heavy = A->piece_heavy;
+    a.variant = A->kernel;
     return a;
 }
 

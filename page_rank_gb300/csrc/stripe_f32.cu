@@ -1,5 +1,6 @@
 // FP32 instances of the fused stripe kernel (SpMM and power-iteration step).
 #include "stripe_launch.cuh"
+#include "window_kernel.cuh"
 
 namespace gl {
 
@@ -8,6 +9,11 @@ template <bool PPR, int BR>
 int dispatch_f32(const StripeArgs<float>& a, int tile_hint, int lane_split, cudaStream_t st) {
     // the half-warp shape is register-heavy with the power-iteration
     // epilogue, so only the plain SpMM uses it
+    if constexpr (!PPR) {
+        // the window kernel (staged X windows) unless the stripe kernel is
+        // asked for or a column tile / lane split other than its own is
+        if (a.variant == 2 && tile_hint <= 0 && lane_split == 0 && window_eligible(a)) return launch_window<BR>(a, st);
+    }
     const Shape sh = pick_shape<float>(a.K, tile_hint, a.X, a.Y, !PPR, lane_split);
     if constexpr (!PPR) {
         if (sh.V == 4 && sh.C == 16) return launch_stripe_shape<float, BR, 4, 16, PPR>(a, st);

@@ -115,6 +115,7 @@ struct StripeArgs {
     const double* col_tol;         // [K] or nullptr: tol for every column
     int32_t cta_sums;              // 1: per-column sums gathered per CTA in shared memory (2 * K doubles
                                    //    after the stripe buffers), one global atomic per CTA and column
+    int32_t variant;               // gl_pbr_matrix.kernel: 0 automatic, 1 stripe kernel, 2 window kernel
 };
 
 template <typename S, int V>

@@ -21,14 +21,20 @@ int launch_stripe_shape(const StripeArgs<S>& a0, cudaStream_t stream) {
     constexpr int64_t kCtaSumCols = 512;
     a.cta_sums = (PPR && a.K <= kCtaSumCols) ? 1 : 0;
     const size_t smem = base + (a.cta_sums ? (size_t)(2 * a.K) * sizeof(double) : 0);
-    static int occ = 0;
-    if (occ == 0) {
-        const size_t most = base + (PPR ? (size_t)(2 * kCtaSumCols) * sizeof(double) : 0);
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
-        int o = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, kStripeThreads, most);
-        occ = o > 0 ? o : 1;
-    }
+    // the shared-memory attribute is per device, so it is set (and the
+    // occupancy measured) once for every device that launches this instance
+    static std::atomic<int> occ_cache[kMaxDevices];
+    int occ = 0;
+    const int rc = per_device_value(
+        occ_cache,
+        [&](int* o) {
+            const size_t most = base + (PPR ? (size_t)(2 * kCtaSumCols) * sizeof(double) : 0);
+            GL_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most));
+            GL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, kern, kStripeThreads, most));
+            return GL_OK;
+        },
+        &occ);
+    if (rc != GL_OK) return rc;
     int64_t blocks = ceil_div(items, kStripeWarps);
     const int64_t cap = (int64_t)num_sms() * occ;
     if (blocks > cap) blocks = cap;

@@ -329,6 +329,7 @@ def _array_desc(meta: dict, rows: int, cols: int, block_rows: int, block_cols: i
     d.stripe_block_ptr = _ptr(meta["stripe_ptr"])
     d.column_tile = int(meta.get("column_tile", 0))
     d.lane_split = int(meta.get("lane_split", 0))
+    d.kernel = int(meta.get("kernel", 0))
     return d
 
 

@@ -10,8 +10,9 @@ columns; dangling sources simply have empty columns.
 * :func:`sbm_graph`      — stochastic block model (64 x 64, p_in 0.1, p_out 5e-4)
 * :func:`cluster_rmat_graph` — 2**20 nodes in clusters of 64, mean out-degree
   16, 70% uniform in-cluster targets, 30% R-MAT (0.57, 0.19, 0.19, 0.05)
-* :func:`cluster_zipf_graph` — Zipf(2.1) out-degrees scaled to a mean, 80% of
-  edges inside the source's 64-node cluster
+* :func:`cluster_zipf_graph` — Zipf(2.1) out-degrees scaled so the mean
+  distinct out-degree is the stated one, 80% of a node's edges to distinct
+  targets inside its 64-node cluster
 * :func:`seed_sets`      — per-column uniform seed sets of random sizes
 """
 from __future__ import annotations
@@ -123,21 +124,65 @@ def cluster_rmat_graph(log2n: int = 20, cluster: int = 64, mean_degree: int = 16
                                f"R-MAT{tuple(rmat)}, seed={seed}", device=device)
 
 
-def cluster_zipf_graph(log2n: int = 22, mean_degree: float = 20.0, zipf_a: float = 2.1, cluster: int = 64,
-                       p_intra: float = 0.8, seed: int = 3, device=None) -> Graph:
+def _zipf_scale(z: np.ndarray, target: float, p_intra: float, cluster: int, n: int) -> float:
+    """Scale s for degrees d_i = max(1, round(s z_i)) such that the expected
+    number of distinct out-neighbours, min(round(p_intra d_i), cluster) +
+    (d_i - round(p_intra d_i)), averages ``target`` (bisection)."""
+    def mean_distinct(scale):
+        d = np.minimum(np.maximum(1, np.round(z * scale)), n - 1)
+        di = np.round(p_intra * d)
+        return float((np.minimum(di, cluster) + (d - di)).mean())
+
+    lo, hi = 0.0, target / max(z.mean(), 1e-12)
+    while mean_distinct(hi) < target:
+        hi *= 2.0
+    for _ in range(60):
+        mid = 0.5 * (lo + hi)
+        if mean_distinct(mid) < target:
+            lo = mid
+        else:
+            hi = mid
+    return hi
+
+
+def cluster_zipf_edges(log2n: int = 22, mean_degree: float = 20.0, zipf_a: float = 2.1, cluster: int = 64,
+                       p_intra: float = 0.8, seed: int = 3) -> tuple[np.ndarray, np.ndarray]:
+    """(source, target) edges of :func:`cluster_zipf_graph`.
+
+    Out-degrees follow Zipf(zipf_a), scaled so that the mean number of
+    *distinct* out-neighbours is ``mean_degree``.  A node's p_intra share of
+    its edges goes to distinct targets inside its own ``cluster``-node cluster
+    (a random arithmetic progression with an odd step modulo the cluster
+    size, at most ``cluster`` of them); the rest go to uniform targets across
+    the graph (repeats there are rare and summed)."""
     rng = np.random.default_rng(seed)
     n = 1 << log2n
     z = rng.zipf(zipf_a, n).astype(np.float64)
     z = np.minimum(z, n)           # a single draw can exceed n
-    deg = np.maximum(1, np.round(z * mean_degree / z.mean())).astype(np.int64)
-    deg = np.minimum(deg, n - 1)
-    src = np.repeat(np.arange(n, dtype=np.int64), deg)
-    m = len(src)
-    intra = rng.random(m) < p_intra
-    dst = np.where(intra, (src // cluster) * cluster + rng.integers(0, cluster, m), rng.integers(0, n, m))
+    scale = _zipf_scale(z, mean_degree, p_intra, cluster, n)
+    deg = np.minimum(np.maximum(1, np.round(z * scale)), n - 1).astype(np.int64)
+    k_in = np.minimum(np.round(p_intra * deg).astype(np.int64), cluster)
+    k_out = deg - np.round(p_intra * deg).astype(np.int64)
+    # intra-cluster targets: base + (offset + j * step) mod cluster, j < k_in
+    src_i = np.repeat(np.arange(n, dtype=np.int64), k_in)
+    first = np.cumsum(k_in) - k_in
+    j = np.arange(src_i.size, dtype=np.int64) - np.repeat(first, k_in)
+    offset = rng.integers(0, cluster, n)
+    step = 2 * rng.integers(0, cluster // 2, n) + 1
+    dst_i = (src_i // cluster) * cluster + (np.repeat(offset, k_in) + j * np.repeat(step, k_in)) % cluster
+    src_o = np.repeat(np.arange(n, dtype=np.int64), k_out)
+    dst_o = rng.integers(0, n, src_o.size)
+    return np.concatenate([src_i, src_o]), np.concatenate([dst_i, dst_o])
+
+
+def cluster_zipf_graph(log2n: int = 22, mean_degree: float = 20.0, zipf_a: float = 2.1, cluster: int = 64,
+                       p_intra: float = 0.8, seed: int = 3, device=None) -> Graph:
+    src, dst = cluster_zipf_edges(log2n, mean_degree, zipf_a, cluster, p_intra, seed)
+    n = 1 << log2n
     return edges_to_transition(src, dst, n,
-                               f"n=2^{log2n}, Zipf({zipf_a}) out-degree scaled to mean {mean_degree}, "
-                               f"{int(p_intra * 100)}% within {cluster}-node clusters, seed={seed}",
+                               f"n=2^{log2n}, Zipf({zipf_a}) out-degree, mean distinct out-degree "
+                               f"{mean_degree:g}, {int(p_intra * 100)}% of each node's edges to distinct "
+                               f"targets in its {cluster}-node cluster, seed={seed}",
                                device=device)
 
 
