@@ -87,6 +87,10 @@ typedef struct gl_pbr_matrix {
      * (see gl_pbr_spmm; falls back to the stripe kernel where it does not
      * apply).  Added in ABI version 101. */
     int32_t kernel;
+    /* [num_pieces][4]: each piece's first and end block and first and end
+     * remainder entry, filled by gl_pbr_schedule_build (NULL: the kernels
+     * find them by binary search).  Added in ABI version 101. */
+    const int32_t* piece_range;
 } gl_pbr_matrix;
 
 /* ======================================================================== */
@@ -190,8 +194,42 @@ int64_t gl_pbr_schedule_elems(const gl_pbr_matrix* A, int32_t piece_work);
 
 /* Builds the load-balance schedule of A into `buffer` (device int32,
  * gl_pbr_schedule_elems() entries) and sets A's schedule fields to point into
- * it.  piece_work <= 0 selects the default (256).  Synchronizes `stream`. */
+ * it.  piece_work <= 0 selects the default (192).  Synchronizes `stream`. */
 int gl_pbr_schedule_build(gl_pbr_matrix* A, int32_t piece_work, int32_t* buffer, int64_t buffer_elems,
+                          cudaStream_t stream);
+
+/* ======================================================================== */
+/* PBR format tools                                                         */
+/* ======================================================================== */
+/* Device workspace (bytes) for gl_pbr_to_csr; -1 when the CSR would not fit
+ * int32 indices. */
+int64_t gl_pbr_to_csr_workspace_bytes(const gl_pbr_matrix* A);
+
+/* PBR -> CSR on the device.  Replaces pbr_to_csr (pbr_matrix/pbr_matrix.cpp:
+ * 289-338, bound at bindings/bindings.cpp:75-78): every block value pairs with
+ * its code's set bits in row-major bit order, remainder entries keep their
+ * rows, and each row comes out sorted by column.  indptr: [rows + 1],
+ * indices / data: [packed_nnz + remainder_nnz] (data of A->value_type).
+ * Rows that are not a multiple of block_rows are handled (the reference
+ * throws there, pbr_matrix.cpp:308-310).  Only stripe_block_ptr and the
+ * schedule fields of A are not read.  Asynchronous on `stream`. */
+int gl_pbr_to_csr(const gl_pbr_matrix* A, int32_t* indptr, int32_t* indices, void* data,
+                  void* workspace, int64_t workspace_bytes, cudaStream_t stream);
+
+/* Device workspace (bytes) for gl_pbr_block_patterns; -1 for too many blocks. */
+int64_t gl_pbr_block_patterns_workspace_bytes(int64_t num_blocks);
+
+/* Block-pattern histogram (what the reference's pbr_analyze_csr,
+ * pbr_matrix.cpp:71-156, computes from a stripe walk): the distinct codes
+ * among block_codes, ascending as unsigned 64-bit values, into
+ * unique_codes / counts (room for num_blocks each), their number into
+ * *num_unique (device int64), and under the coverage rule "occurrences x bit
+ * count >= min_nnz_coverage" (pbr_matrix.cpp:127-141) the device int64
+ * totals[4] = { nnz of compressed patterns, nnz of the others, compressed
+ * patterns, blocks of compressed patterns }.  Asynchronous on `stream`. */
+int gl_pbr_block_patterns(const int64_t* block_codes, int64_t num_blocks, int64_t min_nnz_coverage,
+                          uint64_t* unique_codes, int64_t* counts, int64_t* num_unique,
+                          int64_t* totals, void* workspace, int64_t workspace_bytes,
                           cudaStream_t stream);
 
 /* ======================================================================== */
@@ -207,7 +245,7 @@ int gl_pbr_schedule_build(gl_pbr_matrix* A, int32_t piece_work, int32_t* buffer,
  *
  * Two kernels implement it.  The window kernel (FP32, features % 4 == 0 and
  * >= 64, 16-byte aligned X and Y, a workspace, a schedule built with
- * piece_work <= 256, cols < 2^29) stages the 64 X rows of each 64-row window
+ * piece_work <= 192, cols * features / 4 < 2^29) stages the 64 X rows of each 64-row window
  * in shared memory with bulk asynchronous copies and reads the nonzeros of
  * the window's diagonal block from there; every other case runs the stripe
  * kernel.  A->kernel selects one explicitly.  The window kernel records a

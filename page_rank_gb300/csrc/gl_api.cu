@@ -61,9 +61,15 @@ StripeArgs<S> make_args(const gl_pbr_matrix* A) {
     a.heavy_stripe = A->heavy_stripe;
     a.heavy_first = A->heavy_first;
     a.piece_heavy = A->piece_heavy;
+    a.piece_range = a.num_pieces ? A->piece_range : nullptr;
     a.variant = A->kernel;
     return a;
 }
+
+// Default piece size of the load-balance schedule: stripes above twice this
+// many stored entries are cut into pieces.  192 keeps every other stripe
+// within the window kernel's 384-entry lists.
+constexpr int32_t kDefaultPieceWork = 192;
 
 int64_t workspace_bytes(const gl_pbr_matrix* A, int64_t batch, int64_t K) {
     return workspace_layout(A, batch, K).total;
@@ -87,6 +93,33 @@ int bind_workspace(StripeArgs<S>& a, const gl_pbr_matrix* A, int64_t batch, int6
     a.counters = reinterpret_cast<int32_t*>(base + w.counters);
     a.partial = reinterpret_cast<S*>(base + w.partial);
     return GL_OK;
+}
+
+// Block and remainder range of every piece of a heavy stripe: the stripe's
+// stored entries (packed values, then remainder entries) cut every W
+// entries, the block range rounded to whole blocks by the first block whose
+// offset reaches the cut (so a block belongs to the piece its first value
+// falls in).
+__global__ void piece_range_kernel(const int32_t* stripe_ptr, const int32_t* offsets, const int32_t* rem_ptr,
+                                   int64_t rows, int br, const int32_t* piece_heavy, const int32_t* heavy_stripe,
+                                   const int32_t* heavy_first, int64_t np, int32_t W, int32_t* range) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const int32_t h = piece_heavy[p];
+    const int64_t s = heavy_stripe[h];
+    const int32_t pidx = (int32_t)(p - heavy_first[h]);
+    const int32_t sb0 = stripe_ptr[s], sb1 = stripe_ptr[s + 1];
+    const int64_t pk0 = offsets[sb0];
+    const int64_t pw = (int64_t)offsets[sb1] - pk0;
+    const int64_t last_row = (s * br + br < rows) ? s * br + br : rows;
+    const int32_t rj0 = rem_ptr[s * br], rj1 = rem_ptr[last_row];
+    const int64_t total = pw + (rj1 - rj0);
+    const int64_t u0 = (int64_t)pidx * W;
+    const int64_t u1 = (u0 + W < total) ? u0 + W : total;
+    range[4 * p + 0] = lower_bound_i32(offsets, sb0, sb1, pk0 + u0);
+    range[4 * p + 1] = (u1 >= pw) ? sb1 : lower_bound_i32(offsets, sb0, sb1, pk0 + u1);
+    range[4 * p + 2] = rj0 + (int32_t)(u0 > pw ? u0 - pw : 0);
+    range[4 * p + 3] = rj0 + (int32_t)(u1 > pw ? u1 - pw : 0);
 }
 
 __global__ void stripe_work_kernel(const int32_t* stripe_ptr, const int32_t* offsets, const int32_t* rem_ptr,
@@ -243,15 +276,17 @@ extern "C" int64_t gl_pbr_spmm_workspace_bytes(const gl_pbr_matrix* A, int64_t b
 
 extern "C" int64_t gl_pbr_schedule_elems(const gl_pbr_matrix* A, int32_t piece_work) {
     if (A == nullptr || A->block_rows < 1) return -1;
-    const int64_t w = piece_work > 0 ? piece_work : 256;
+    const int64_t w = piece_work > 0 ? piece_work : kDefaultPieceWork;
     const int64_t ns = ceil_div(A->rows, A->block_rows);
-    return 4 * ns + 8 + (A->packed_nnz + A->remainder_nnz) / w;
+    // heavy_of [ns], heavy_stripe [H], heavy_first [H + 1], piece_heavy [NP],
+    // 16-byte padding, piece_range [4 NP]; H <= ns, NP <= (packed + rem) / w + H
+    return 8 * ns + 16 + 5 * ((A->packed_nnz + A->remainder_nnz) / w);
 }
 
 extern "C" int gl_pbr_schedule_build(gl_pbr_matrix* A, int32_t piece_work, int32_t* buffer, int64_t buffer_elems,
                                      cudaStream_t stream) {
     GL_REQUIRE(A != nullptr && A->block_rows >= 1, GL_ERR_INVALID_ARGUMENT, "bad matrix");
-    const int32_t W = piece_work > 0 ? piece_work : 256;
+    const int32_t W = piece_work > 0 ? piece_work : kDefaultPieceWork;
     const int64_t need = gl_pbr_schedule_elems(A, W);
     GL_REQUIRE(buffer != nullptr && buffer_elems >= need, GL_ERR_WORKSPACE, "schedule buffer of %lld int32 needed",
                (long long)need);
@@ -260,6 +295,7 @@ extern "C" int gl_pbr_schedule_build(gl_pbr_matrix* A, int32_t piece_work, int32
     A->num_pieces = 0;
     A->piece_work = W;
     A->heavy_of = nullptr;
+    A->piece_range = nullptr;
     if (ns == 0) return GL_OK;
     stripe_work_kernel<<<(unsigned)ceil_div(ns, 256), 256, 0, stream>>>(A->stripe_block_ptr, A->block_offsets,
                                                                         A->remainder_indptr, A->rows, A->block_rows,
@@ -281,15 +317,23 @@ extern "C" int gl_pbr_schedule_build(gl_pbr_matrix* A, int32_t piece_work, int32
     }
     const int64_t H = (int64_t)heavy_stripe.size(), NP = (int64_t)piece_heavy.size();
     if (H == 0) return GL_OK;
-    GL_REQUIRE(ns + H + (H + 1) + NP <= buffer_elems, GL_ERR_WORKSPACE, "schedule buffer too small");
+    const int64_t range_off = (ns + H + (H + 1) + NP + 3) / 4 * 4;   // 16-byte aligned (int4 loads)
+    GL_REQUIRE(range_off + 4 * NP <= buffer_elems, GL_ERR_WORKSPACE, "schedule buffer too small");
+    GL_REQUIRE(reinterpret_cast<uintptr_t>(buffer) % 16 == 0, GL_ERR_INVALID_ARGUMENT,
+               "schedule buffer must be 16-byte aligned");
     int32_t* d_heavy_of = buffer;
     int32_t* d_heavy_stripe = d_heavy_of + ns;
     int32_t* d_heavy_first = d_heavy_stripe + H;
     int32_t* d_piece_heavy = d_heavy_first + H + 1;
+    int32_t* d_piece_range = buffer + range_off;
     GL_CUDA_TRY(cudaMemcpyAsync(d_heavy_of, heavy_of.data(), 4 * ns, cudaMemcpyHostToDevice, stream));
     GL_CUDA_TRY(cudaMemcpyAsync(d_heavy_stripe, heavy_stripe.data(), 4 * H, cudaMemcpyHostToDevice, stream));
     GL_CUDA_TRY(cudaMemcpyAsync(d_heavy_first, heavy_first.data(), 4 * (H + 1), cudaMemcpyHostToDevice, stream));
     GL_CUDA_TRY(cudaMemcpyAsync(d_piece_heavy, piece_heavy.data(), 4 * NP, cudaMemcpyHostToDevice, stream));
+    piece_range_kernel<<<(unsigned)ceil_div(NP, 256), 256, 0, stream>>>(
+        A->stripe_block_ptr, A->block_offsets, A->remainder_indptr, A->rows, A->block_rows, d_piece_heavy,
+        d_heavy_stripe, d_heavy_first, NP, W, d_piece_range);
+    GL_LAUNCH_CHECK("piece_range_kernel");
     GL_CUDA_TRY(cudaStreamSynchronize(stream));
     A->num_heavy = (int32_t)H;
     A->num_pieces = (int32_t)NP;
@@ -297,6 +341,7 @@ extern "C" int gl_pbr_schedule_build(gl_pbr_matrix* A, int32_t piece_work, int32
     A->heavy_stripe = d_heavy_stripe;
     A->heavy_first = d_heavy_first;
     A->piece_heavy = d_piece_heavy;
+    A->piece_range = d_piece_range;
     return GL_OK;
 }
 

@@ -80,6 +80,7 @@ StripeArgs<S> static_args(const gl_pbr_matrix* A, const void* X, void* Y, int64_
     a.heavy_stripe = A->heavy_stripe;
     a.heavy_first = A->heavy_first;
     a.piece_heavy = A->piece_heavy;
+    a.piece_range = a.num_pieces ? A->piece_range : nullptr;
     a.variant = A->kernel;
     return a;
 }

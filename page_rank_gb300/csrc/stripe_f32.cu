@@ -10,8 +10,8 @@ int dispatch_f32(const StripeArgs<float>& a, int tile_hint, int lane_split, cuda
     // the half-warp shape is register-heavy with the power-iteration
     // epilogue, so only the plain SpMM uses it
     if constexpr (!PPR) {
-        // the window kernel (staged X windows) unless the stripe kernel is
-        // asked for or a column tile / lane split other than its own is
+        // the window kernel (staged X windows) when asked for and its shape
+        // applies (no other column tile / lane split)
         if (a.variant == 2 && tile_hint <= 0 && lane_split == 0 && window_eligible(a)) return launch_window<BR>(a, st);
     }
     const Shape sh = pick_shape<float>(a.K, tile_hint, a.X, a.Y, !PPR, lane_split);

@@ -92,6 +92,7 @@ struct StripeArgs {
     const int32_t* heavy_stripe;   // [num_heavy]
     const int32_t* heavy_first;    // [num_heavy + 1]
     const int32_t* piece_heavy;    // [num_pieces]
+    const int32_t* piece_range;    // [num_pieces][4] block / remainder ranges, or nullptr
     S* partial;                    // [num_pieces][batch * ntiles][BR][T]
     int32_t* counters;             // [num_heavy][batch * ntiles], zero between calls
     // work distribution: units are drawn one at a time from sched[0];
@@ -880,14 +881,22 @@ stripe_kernel(const StripeArgs<S> a) {
             const int64_t last_row = (s * BR + BR < a.rows) ? s * BR + BR : a.rows;
             const int32_t rj0 = a.rem_ptr[s * BR], rj1 = a.rem_ptr[last_row];
             const int64_t total = pw + (rj1 - rj0);
-            const int64_t u0 = (int64_t)pidx * a.piece_work;
-            const int64_t u1 = (u0 + a.piece_work < total) ? u0 + a.piece_work : total;
-            b0 = lower_bound_i32(a.offsets, sb0, sb1, pk0 + u0);
-            b1 = (u1 >= pw) ? sb1 : lower_bound_i32(a.offsets, sb0, sb1, pk0 + u1);
-            const int64_t r0 = u0 > pw ? u0 - pw : 0;
-            const int64_t r1 = u1 > pw ? u1 - pw : 0;
-            j0 = rj0 + (int32_t)r0;
-            j1 = rj0 + (int32_t)r1;
+            if (a.piece_range != nullptr) {
+                const int4 pr = *reinterpret_cast<const int4*>(a.piece_range + 4 * u);
+                b0 = pr.x;
+                b1 = pr.y;
+                j0 = pr.z;
+                j1 = pr.w;
+            } else {
+                const int64_t u0 = (int64_t)pidx * a.piece_work;
+                const int64_t u1 = (u0 + a.piece_work < total) ? u0 + a.piece_work : total;
+                b0 = lower_bound_i32(a.offsets, sb0, sb1, pk0 + u0);
+                b1 = (u1 >= pw) ? sb1 : lower_bound_i32(a.offsets, sb0, sb1, pk0 + u1);
+                const int64_t r0 = u0 > pw ? u0 - pw : 0;
+                const int64_t r1 = u1 > pw ? u1 - pw : 0;
+                j0 = rj0 + (int32_t)r0;
+                j1 = rj0 + (int32_t)r1;
+            }
         } else {
             // every load of the stripe's setup issued before the first use
             // (one memory round trip): heavy flag, block range, and the

@@ -7,31 +7,33 @@
 // the same kWinRows columns: the 2^20-node clustered R-MAT graph has 68.6 %
 // of its nonzeros in the aligned 64 x 64 diagonal window.  Those X rows are
 // staged once per window into shared memory by a bulk asynchronous copy
-// (cp.async.bulk, completion on an mbarrier, double-buffered), so two thirds
-// of the per-nonzero X-row reads come from shared memory instead of a
-// ~1 us L2 / HBM round trip; the rest are gathered from global memory in
+// (cp.async.bulk, completion on an mbarrier, kWinBufs windows in flight), so
+// two thirds of the per-nonzero X-row reads come from shared memory instead
+// of an L2 / HBM round trip; the rest are gathered from global memory in
 // deep batches.
 //
 // Roles (kWinWarps + 1 warps per CTA):
 //   * the producer warp draws work units from a global counter (so CTAs
-//     balance dynamically), and for each one issues the bulk copy of the
-//     window's X tile into the free buffer; unit number and window base go
-//     to shared memory next to the buffer;
-//   * each consumer warp takes stripes of the window (or one piece of a
-//     heavy stripe): it decodes the stripe's bitmask blocks and remainder
-//     entries into a list of (column, row, value) entries in shared memory —
-//     entries whose column lies in the staged window at the front, the others
-//     at the back — walks the global entries in batches of kWinGather X-row
-//     gathers per half-warp, then the window entries from shared memory,
-//     committing each row's sum to its half-warp's tile, and writes every Y
-//     row once (no atomics, no pre-zeroed Y).
+//     balance dynamically); for each one it reads the window's stripe and row
+//     pointers into shared memory and issues the bulk copy of the window's X
+//     tile into the free buffer;
+//   * the consumer warps take the unit's items (stripes of the window, or
+//     pieces of heavy stripes) one at a time from a shared counter, so a
+//     slow stripe does not hold the other warps back.  A warp decodes its
+//     item's bitmask blocks and remainder entries into a list of (X-row
+//     offset, row, value) entries in shared memory — entries whose column lies
+//     in the staged window at the front, the others at the back — walks the
+//     global entries in batches of kWinGather X-row gathers per half-warp,
+//     then the window entries from shared memory, committing each row's sum
+//     to its half-warp's tile, and writes every Y row once (no atomics, no
+//     pre-zeroed Y).
 //
 // Half-warps: lanes 0-15 and 16-31 each cover the 64 columns of the tile
 // with float4 lanes and take alternate entries; each has its own tile, and a
 // row's result is tile0 + tile1 in that order, so results are deterministic.
 // Heavy stripes (more than 2 x piece_work stored entries) are cut into
-// pieces exactly as in the stripe kernel (partial tiles in the workspace,
-// reduced in piece order by the last piece to finish).
+// pieces as in the stripe kernel (partial tiles in the workspace, reduced in
+// piece order by the last piece to finish).
 //
 // Every wait on an mbarrier is bounded (about two seconds of SM clock); a
 // wait that gives up records GL_ERR_TIMEOUT in the workspace's error word and
@@ -46,27 +48,43 @@ constexpr int kWinRows = 64;                      // rows per window = X rows st
 constexpr int kWinWarps = 8;                      // consumer warps
 constexpr int kWinThreads = (kWinWarps + 1) * 32; // + the producer warp
 constexpr int kWinCols = 64;                      // columns per tile: 16 lanes x float4
-constexpr int kWinList = 512;                     // list entries per warp (>= 2 x the largest piece_work)
+#ifndef GL_WIN_BUFS
+#define GL_WIN_BUFS 3
+#endif
+#ifndef GL_WIN_PREFETCH_INFO
+#define GL_WIN_PREFETCH_INFO 1
+#endif
+#ifndef GL_WIN_DYNAMIC_ITEMS
+#define GL_WIN_DYNAMIC_ITEMS 1
+#endif
+#ifndef GL_WIN_MAXREG
+#define GL_WIN_MAXREG 96
+#endif
+constexpr int kWinBufs = GL_WIN_BUFS;             // X windows in flight per CTA
+constexpr int kWinList = 384;                     // list entries per warp (>= 2 x the largest piece_work)
 constexpr int kWinMaxPieceWork = kWinList / 2;
+constexpr int kWinInfo = 136;                     // per buffer: stripe pointers, heavy flags, row pointers
 #ifndef GL_WIN_GATHER
 #define GL_WIN_GATHER 8
 #endif
 constexpr int kWinGather = GL_WIN_GATHER;         // global X-row gathers in flight per half-warp
 constexpr long long kWinTimeoutCycles = 4000000000LL;
 
-// Shared memory of one CTA (dynamic, 128-byte aligned regions).
+// Shared memory of one CTA (dynamic; every region 16-byte aligned).
 template <int BR>
 struct WinSmem {
-    static constexpr size_t xwin = 0;                                                   // [2][rows][64] f32
-    static constexpr size_t xwin_bytes = 2ull * kWinRows * kWinCols * 4;
+    static constexpr size_t xwin = 0;                                                   // [bufs][rows][64] f32
+    static constexpr size_t xwin_bytes = (size_t)kWinBufs * kWinRows * kWinCols * 4;
     static constexpr size_t lists = xwin + xwin_bytes;                                  // [warps][list] uint2
     static constexpr size_t lists_bytes = (size_t)kWinWarps * kWinList * 8;
     static constexpr size_t tiles = lists + lists_bytes;                                // [warps][2][BR][64]
     static constexpr size_t tiles_bytes = (size_t)kWinWarps * 2 * BR * kWinCols * 4;
     static constexpr size_t rinfo = tiles + tiles_bytes;                                // [warps][16] i32
     static constexpr size_t rinfo_bytes = (size_t)kWinWarps * 16 * 4;
-    static constexpr size_t ctl = rinfo + rinfo_bytes;                                  // barriers, unit ids
-    static constexpr size_t bytes = ctl + 64;
+    static constexpr size_t winfo = rinfo + rinfo_bytes;                                // [bufs][kWinInfo] i32
+    static constexpr size_t winfo_bytes = (size_t)kWinBufs * kWinInfo * 4;
+    static constexpr size_t ctl = winfo + winfo_bytes;                                  // barriers, unit ids
+    static constexpr size_t bytes = ctl + 128;
 };
 
 // ---- mbarrier / bulk-copy helpers (inline PTX) -----------------------------
@@ -114,9 +132,12 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
 }
 
 // ---- list walking ------------------------------------------------------------
-// One list entry: key = (column << 3) | row-in-stripe (window entries hold
-// the column relative to the window), value bits.
-__device__ __forceinline__ uint32_t win_key(uint32_t col, int r) { return (col << 3) | (uint32_t)r; }
+// One list entry: key = (float4 index of the X row << 3) | row-in-stripe and
+// the value's bits.  The float4 index is column * K / 4 into X for global
+// entries and column-in-window * 16 into the staged window for the others,
+// so a lane's address is its base pointer + index (one shift, one
+// multiply-add).
+__device__ __forceinline__ uint32_t win_key(uint32_t f4, int r) { return (f4 << 3) | (uint32_t)r; }
 
 __device__ __forceinline__ void win_fma(float4& acc, float v, const float4& x) {
     float2 a = make_float2(acc.x, acc.y), b = make_float2(acc.z, acc.w);
@@ -144,45 +165,61 @@ __device__ __forceinline__ void win_commit(float* ht, int r, const float4& acc, 
     }
 }
 
+// One entry of a walk: a row change commits the running sum.
+__device__ __forceinline__ void win_step(const uint2& en, const float4& x, float4& acc, int& cur, float* ht,
+                                         uint32_t& touched) {
+    const int r = (int)(en.x & 7u);
+    if (r != cur) {
+        if (cur >= 0) win_commit(ht, cur, acc, touched);
+        acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        cur = r;
+    }
+    win_fma(acc, __uint_as_float(en.y), x);
+}
+
 // Walks entries [0, n) of a list segment: half-warp h takes entries h, h + 2,
-// ...; NB X-row loads are issued before their FMAs.  src points at column
-// 4 * (lane % 16) of X row 0 (global) or of the staged window (shared), ld is
-// the row stride in floats.
+// ...; NB X-row loads are issued before their FMAs (full batches without
+// predicates, then one predicated tail).  base: the lane's float4 pointer
+// into X (global) or into the staged window (shared).
 template <int NB>
-__device__ __forceinline__ void win_walk(const uint2* lst, int n, const float* src, int64_t ld, float* ht,
+__device__ __forceinline__ void win_walk(const uint2* lst, int n, const float4* base, float* ht,
                                          uint32_t& touched, int h) {
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     int cur = -1;
-    for (int base = 0; base < n; base += 2 * NB) {
+    int e0 = 0;
+    for (; e0 + 2 * NB <= n; e0 += 2 * NB) {
+        uint2 en[NB];
         float4 x[NB];
 #pragma unroll
         for (int q = 0; q < NB; ++q) {
-            const int e = base + 2 * q + h;
-            x[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (e < n) x[q] = *reinterpret_cast<const float4*>(src + (int64_t)(lst[e].x >> 3) * ld);
+            en[q] = lst[e0 + 2 * q + h];
+            x[q] = base[en[q].x >> 3];
         }
 #pragma unroll
+        for (int q = 0; q < NB; ++q) win_step(en[q], x[q], acc, cur, ht, touched);
+    }
+    if (e0 < n) {
+        uint2 en[NB];
+        float4 x[NB];
+#pragma unroll
         for (int q = 0; q < NB; ++q) {
-            const int e = base + 2 * q + h;
+            const int e = e0 + 2 * q + h;
             if (e < n) {
-                const uint2 en = lst[e];
-                const int r = (int)(en.x & 7u);
-                if (r != cur) {
-                    if (cur >= 0) win_commit(ht, cur, acc, touched);
-                    acc = make_float4(0.f, 0.f, 0.f, 0.f);
-                    cur = r;
-                }
-                win_fma(acc, __uint_as_float(en.y), x[q]);
+                en[q] = lst[e];
+                x[q] = base[en[q].x >> 3];
             }
         }
+#pragma unroll
+        for (int q = 0; q < NB; ++q)
+            if (e0 + 2 * q + h < n) win_step(en[q], x[q], acc, cur, ht, touched);
     }
     if (cur >= 0) win_commit(ht, cur, acc, touched);
 }
 
-// Decodes one unit (the blocks [b0, b1) and remainder entries [j0, j1) of
-// stripe s; rstart[0..BR] in shared memory holds each row's first remainder
+// Decodes one item (the blocks [b0, b1) and remainder entries [j0, j1) of
+// a stripe; rstart[0..BR] in shared memory holds each row's first remainder
 // entry, clamped to [j0, j1]) into the warp's list and accumulates it into
-// the two half-warp tiles.  Returns false if the unit has more entries than
+// the two half-warp tiles.  Returns false if the item has more entries than
 // the list holds (the caller records an error).
 template <int BR>
 __device__ __forceinline__ bool win_unit(const StripeArgs<float>& a, int32_t b0, int32_t b1, int32_t j0, int32_t j1,
@@ -193,6 +230,7 @@ __device__ __forceinline__ bool win_unit(const StripeArgs<float>& a, int32_t b0,
     constexpr int NS = 2 * BR;   // row slots: [0, BR) window entries, [BR, 2 BR) global entries
     using RP = RowPack<NS>;
     const int h = lane >> 4;
+    const uint32_t K4 = (uint32_t)(a.K >> 2);
     const int nrem = j1 - j0;
     // first two rounds of remainder entries in flight with the block metadata
     int32_t rcol[2];
@@ -272,7 +310,10 @@ __device__ __forceinline__ bool win_unit(const StripeArgs<float>& a, int32_t b0,
                 for (int rr = 0; rr < BR - 1; ++rr)
                     rowstart += rr < r ? (int)(bloc ? tot.get(rr) : tot.get(BR + rr)) : 0;
                 const int pos0 = (bloc ? lpos : gbase) + rowstart + within;
-                const uint32_t kb = (uint32_t)(bloc ? bcol0 - xb : bcol0);
+                // float4 index of column c of the block: global (bcol0 + c) * K4,
+                // window (bcol0 - xb + c) * 16
+                const uint32_t f0 = bloc ? (uint32_t)(bcol0 - xb) * 16u : (uint32_t)bcol0 * K4;
+                const uint32_t fs = bloc ? 16u : K4;
                 float v[BC];
                 int q = 0;
 #pragma unroll
@@ -281,7 +322,8 @@ __device__ __forceinline__ bool win_unit(const StripeArgs<float>& a, int32_t b0,
                 q = 0;
 #pragma unroll
                 for (int c = 0; c < BC; ++c)
-                    if ((rb >> c) & 1u) lst[pos0 + q++] = make_uint2(win_key(kb + c, r), __float_as_uint(v[c]));
+                    if ((rb >> c) & 1u)
+                        lst[pos0 + q++] = make_uint2(win_key(f0 + (uint32_t)c * fs, r), __float_as_uint(v[c]));
             }
         }
         lpos += ltot;
@@ -314,10 +356,11 @@ __device__ __forceinline__ bool win_unit(const StripeArgs<float>& a, int32_t b0,
 #pragma unroll
             for (int r2 = 1; r2 < BR; ++r2) r += rstart[r2] <= i ? 1 : 0;
             if (loc) {
-                lst[lpos + __popc(mL & below)] = make_uint2(win_key((uint32_t)(col - xb), r), __float_as_uint(val));
+                lst[lpos + __popc(mL & below)] =
+                    make_uint2(win_key((uint32_t)(col - xb) * 16u, r), __float_as_uint(val));
             } else {
                 lst[kWinList - gpos - __popc(mG) + __popc(mG & below)] =
-                    make_uint2(win_key((uint32_t)col, r), __float_as_uint(val));
+                    make_uint2(win_key((uint32_t)col * K4, r), __float_as_uint(val));
             }
         }
         lpos += __popc(mL);
@@ -327,21 +370,42 @@ __device__ __forceinline__ bool win_unit(const StripeArgs<float>& a, int32_t b0,
     // global entries first (deep gather batches), then the window's
     const int c4 = (lane & 15) * 4;
     float* ht = tile + h * BR * kWinCols + c4;   // this lane's 4 columns of its half-warp's tile
-    win_walk<kWinGather>(lst + (kWinList - gpos), gpos, Xg, a.K, ht, touched, h);
-    win_walk<4>(lst, lpos, xw + c4, kWinCols, ht, touched, h);
+    win_walk<kWinGather>(lst + (kWinList - gpos), gpos, reinterpret_cast<const float4*>(Xg), ht, touched, h);
+    win_walk<4>(lst, lpos, reinterpret_cast<const float4*>(xw + c4), ht, touched, h);
     __syncwarp();
     return true;
 }
 
+// Sum of the two half-warp tiles' row r for this lane's 4 columns (rows a
+// half-warp did not touch count as zero).
 template <int BR>
-__global__ void __launch_bounds__(kWinThreads, 2) window_kernel(const StripeArgs<float> a) {
+__device__ __forceinline__ float4 win_row(const float* tile, int r, int c4, uint32_t t0m, uint32_t t1m) {
+    float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
+    if ((t0m >> r) & 1u) y = *reinterpret_cast<const float4*>(tile + r * kWinCols + c4);
+    if ((t1m >> r) & 1u) {
+        const float4 z = *reinterpret_cast<const float4*>(tile + (BR + r) * kWinCols + c4);
+        y.x += z.x;
+        y.y += z.y;
+        y.z += z.z;
+        y.w += z.w;
+    }
+    return y;
+}
+
+// 96 registers: two CTAs of 288 threads per SM put five warps on one SM
+// sub-partition, whose register file (16 K) then allows at most 102 per
+// thread.
+template <int BR>
+__global__ void __maxnreg__(GL_WIN_MAXREG) window_kernel(const StripeArgs<float> a) {
     using SM = WinSmem<BR>;
     extern __shared__ __align__(128) unsigned char smem[];
     float* const xwin = reinterpret_cast<float*>(smem + SM::xwin);
+    int32_t* const winfo = reinterpret_cast<int32_t*>(smem + SM::winfo);
     uint64_t* const full = reinterpret_cast<uint64_t*>(smem + SM::ctl);
-    uint64_t* const empty = full + 2;
-    int64_t* const unit_of = reinterpret_cast<int64_t*>(full + 4);   // [2]
-    int32_t* const xbase_of = reinterpret_cast<int32_t*>(unit_of + 2);  // [2]
+    uint64_t* const empty = full + kWinBufs;
+    int64_t* const unit_of = reinterpret_cast<int64_t*>(empty + kWinBufs);   // [bufs]
+    int32_t* const xbase_of = reinterpret_cast<int32_t*>(unit_of + kWinBufs); // [bufs]
+    int32_t* const take = xbase_of + kWinBufs;                                // [bufs] items handed out
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -350,13 +414,14 @@ __global__ void __launch_bounds__(kWinThreads, 2) window_kernel(const StripeArgs
     const int64_t nwin = (a.rows + kWinRows - 1) / kWinRows;
     const int64_t units = (npg + nwin) * BT;
     constexpr int SPW = kWinRows / BR;                                 // stripes per window
+    static_assert(SPW + 1 + SPW + kWinRows + 1 <= kWinInfo, "window info fits");
     int32_t* const err = reinterpret_cast<int32_t*>(a.sched + 2);
 
     if (threadIdx.x == 0) {
-        mbar_init(&full[0], 1);
-        mbar_init(&full[1], 1);
-        mbar_init(&empty[0], kWinWarps);
-        mbar_init(&empty[1], kWinWarps);
+        for (int i = 0; i < kWinBufs; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], kWinWarps);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
@@ -364,12 +429,14 @@ __global__ void __launch_bounds__(kWinThreads, 2) window_kernel(const StripeArgs
     if (warp == kWinWarps) {
         // ---- producer ---------------------------------------------------------
         for (int64_t k = 0;; ++k) {
-            const int buf = (int)(k & 1);
-            if (k >= 2 && !mbar_wait(&empty[buf], (uint32_t)(((k >> 1) - 1) & 1))) {
+            const int buf = (int)(k % kWinBufs);
+            const int64_t use = k / kWinBufs;
+            if (use >= 1 && !mbar_wait(&empty[buf], (uint32_t)((use - 1) & 1))) {
                 if (lane == 0) atomicExch(err, GL_ERR_TIMEOUT);
                 // let the copies already issued land before the CTA can exit
-                // (bounded as well): the other buffer's, issued last round
-                mbar_wait(&full[buf ^ 1], (uint32_t)(((k - 1) >> 1) & 1));
+                // (bounded as well)
+                for (int64_t kk = k - kWinBufs + 1; kk < k; ++kk)
+                    if (kk >= 0) mbar_wait(&full[kk % kWinBufs], (uint32_t)((kk / kWinBufs) & 1));
                 break;
             }
             unsigned long long u = 0;
@@ -387,20 +454,42 @@ __global__ void __launch_bounds__(kWinThreads, 2) window_kernel(const StripeArgs
             const int64_t b = bt / a.ntiles;
             const int tile = (int)(bt - b * a.ntiles);
             int64_t xb;
+            int32_t* info = winfo + buf * kWinInfo;
             if (w < npg) {
                 const int32_t hh = a.piece_heavy[w * kWinWarps];
                 xb = ((int64_t)a.heavy_stripe[hh] * BR) / kWinRows * kWinRows;
             } else {
+                // the window's stripe pointers, heavy flags and row pointers,
+                // so the consumers start their stripes from shared memory:
+                // info[0..SPW] stripe_ptr, info[SPW+1..2SPW] heavy_of,
+                // info[2SPW+1..2SPW+1+64] rem_ptr (clamped to the matrix)
                 xb = (w - npg) * kWinRows;
+                const int64_t s0 = xb / BR;
+                for (int i = lane; GL_WIN_PREFETCH_INFO && i < kWinInfo; i += 32) {
+                    int32_t v = 0;
+                    if (i <= SPW) {
+                        const int64_t s = s0 + i < a.nstripes ? s0 + i : a.nstripes;
+                        v = a.stripe_ptr[s];
+                    } else if (i <= 2 * SPW) {
+                        const int64_t s = s0 + (i - SPW - 1);
+                        v = (a.heavy_of != nullptr && s < a.nstripes) ? a.heavy_of[s] : -1;
+                    } else if (i <= 2 * SPW + 1 + kWinRows) {
+                        const int64_t r = xb + (i - 2 * SPW - 1);
+                        v = a.rem_ptr[r < a.rows ? r : a.rows];
+                    }
+                    info[i] = v;
+                }
             }
             const int64_t nx = a.cols - xb < kWinRows ? (a.cols - xb > 0 ? a.cols - xb : 0) : kWinRows;
             const int tw = (a.K - tile * kWinCols) < kWinCols ? (a.K - tile * kWinCols) : kWinCols;
             const uint32_t bytes = (uint32_t)(nx * tw * 4);
             float* dst = xwin + buf * (kWinRows * kWinCols);
             const float* src = a.X + (b * a.cols + xb) * (int64_t)a.K + tile * kWinCols;
+            __syncwarp();
             if (lane == 0) {
                 unit_of[buf] = (int64_t)u;
                 xbase_of[buf] = (int32_t)xb;
+                take[buf] = 0;
                 mbar_arrive_expect_tx(&full[buf], bytes);
             }
             __syncwarp();
@@ -433,138 +522,167 @@ __global__ void __launch_bounds__(kWinThreads, 2) window_kernel(const StripeArgs
     const int c4 = (lane & 15) * 4;
 
     for (int64_t k = 0;; ++k) {
-        const int buf = (int)(k & 1);
-        if (!mbar_wait(&full[buf], (uint32_t)((k >> 1) & 1))) {
+        const int buf = (int)(k % kWinBufs);
+        if (!mbar_wait(&full[buf], (uint32_t)((k / kWinBufs) & 1))) {
             if (lane == 0) atomicExch(err, GL_ERR_TIMEOUT);
             break;
         }
-        const int64_t u = unit_of[buf];
-        if (u < 0) break;
+        const int64_t u64 = unit_of[buf];
+        if (u64 < 0) break;
+        // unit numbers, windows and batch x tile indices fit 32 bits (fewer
+        // live registers across the list walks)
+        const uint32_t u = (uint32_t)u64;
         const int32_t xb = xbase_of[buf];
         const float* xw = xwin + buf * (kWinRows * kWinCols);
-        const int64_t bt = u % BT;
-        const int64_t w = u / BT;
-        const int64_t b = bt / a.ntiles;
-        const int tile_i = (int)(bt - b * a.ntiles);
+        const int32_t* info = winfo + buf * kWinInfo;
+        const uint32_t bt = u % (uint32_t)BT;
+        const int64_t w = (int64_t)(u / (uint32_t)BT);
+        const int32_t b = (int32_t)(bt / (uint32_t)a.ntiles);
+        const int tile_i = (int)(bt - (uint32_t)b * (uint32_t)a.ntiles);
         const int col_base = tile_i * kWinCols + c4;
         const bool lane_ok = col_base < a.K;
-        const float* Xg = a.X + b * a.cols * (int64_t)a.K + (lane_ok ? col_base : tile_i * kWinCols);
+        const float* Xg = a.X + (int64_t)b * a.cols * (int64_t)a.K + (lane_ok ? col_base : tile_i * kWinCols);
+        const bool pieces = w < npg;
+        const int items = pieces ? (int)((a.num_pieces - w * kWinWarps) < kWinWarps ? (a.num_pieces - w * kWinWarps)
+                                                                                    : kWinWarps)
+                                 : SPW;
 
-        if (w < npg) {
-            // ---- one piece of a heavy stripe --------------------------------------
-            const int64_t p = w * kWinWarps + warp;
-            if (p < a.num_pieces) {
+        // items of the unit (stripes of the window, or pieces) are handed out
+        // one at a time to whichever warp asks, so the warps stay balanced
+        for (int it_static = warp;; it_static += kWinWarps) {
+#if GL_WIN_DYNAMIC_ITEMS
+            int it = 0;
+            if (lane == 0) it = atomicAdd(&take[buf], 1);
+            it = __shfl_sync(0xffffffffu, it, 0);
+#else
+            const int it = it_static;
+#endif
+            if (it >= items) break;
+            // the item's ranges; rstart[0..BR] = first remainder entry of each
+            // row, rstart[9] = first row, rstart[10] = rows, rstart[11] = piece
+            // number or -1 (light stripe)
+            int32_t b0, b1, j0, j1;
+            if (pieces) {
+                const int64_t p = w * kWinWarps + it;
                 const int32_t hh = a.piece_heavy[p];
                 const int64_t s = a.heavy_stripe[hh];
-                const int32_t f0 = a.heavy_first[hh];
-                const int32_t npieces = a.heavy_first[hh + 1] - f0;
-                const int32_t pidx = (int32_t)(p - f0);
-                const int32_t sb0 = a.stripe_ptr[s], sb1 = a.stripe_ptr[s + 1];
-                const int64_t pk0 = a.offsets[sb0];
-                const int64_t pw = (int64_t)a.offsets[sb1] - pk0;
                 const int64_t row0 = s * BR;
                 const int nr = (int)(row0 + BR < a.rows ? BR : a.rows - row0);
-                const int32_t rj0 = a.rem_ptr[row0], rj1 = a.rem_ptr[row0 + nr];
-                const int64_t total = pw + (rj1 - rj0);
-                const int64_t u0 = (int64_t)pidx * a.piece_work;
-                const int64_t u1 = (u0 + a.piece_work < total) ? u0 + a.piece_work : total;
-                const int32_t b0 = lower_bound_i32(a.offsets, sb0, sb1, pk0 + u0);
-                const int32_t b1 = (u1 >= pw) ? sb1 : lower_bound_i32(a.offsets, sb0, sb1, pk0 + u1);
-                const int32_t j0 = rj0 + (int32_t)(u0 > pw ? u0 - pw : 0);
-                const int32_t j1 = rj0 + (int32_t)(u1 > pw ? u1 - pw : 0);
+                if (a.piece_range != nullptr) {
+                    const int4 pr = *reinterpret_cast<const int4*>(a.piece_range + 4 * p);
+                    b0 = pr.x;
+                    b1 = pr.y;
+                    j0 = pr.z;
+                    j1 = pr.w;
+                } else {
+                    const int32_t pidx = (int32_t)(p - a.heavy_first[hh]);
+                    const int32_t sb0 = a.stripe_ptr[s], sb1 = a.stripe_ptr[s + 1];
+                    const int64_t pk0 = a.offsets[sb0];
+                    const int64_t pw = (int64_t)a.offsets[sb1] - pk0;
+                    const int32_t rj0 = a.rem_ptr[row0], rj1 = a.rem_ptr[row0 + nr];
+                    const int64_t total = pw + (rj1 - rj0);
+                    const int64_t u0 = (int64_t)pidx * a.piece_work;
+                    const int64_t u1 = (u0 + a.piece_work < total) ? u0 + a.piece_work : total;
+                    b0 = lower_bound_i32(a.offsets, sb0, sb1, pk0 + u0);
+                    b1 = (u1 >= pw) ? sb1 : lower_bound_i32(a.offsets, sb0, sb1, pk0 + u1);
+                    j0 = rj0 + (int32_t)(u0 > pw ? u0 - pw : 0);
+                    j1 = rj0 + (int32_t)(u1 > pw ? u1 - pw : 0);
+                }
                 if (lane <= BR) {
                     int32_t rs = j1;
                     if (lane < nr) rs = a.rem_ptr[row0 + lane];
                     rs = rs < j0 ? j0 : (rs > j1 ? j1 : rs);
                     rstart[lane] = rs;
                 }
-                __syncwarp();
-                uint32_t touched = 0;
-                if (!win_unit<BR>(a, b0, b1, j0, j1, rstart, xb, xw, Xg, lst, tile, touched, lane)) {
-                    if (lane == 0) atomicExch(err, GL_ERR_INVALID_ARGUMENT);
-                } else {
-                    // partial tile -> workspace; the last piece of the stripe reduces
-                    const uint32_t t0m = __shfl_sync(0xffffffffu, touched, 0);
-                    const uint32_t t1m = __shfl_sync(0xffffffffu, touched, 16);
-                    float* part = a.partial + ((int64_t)p * BT + bt) * BR * kWinCols;
-                    for (int r = h; r < BR; r += 2) {
-                        float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
-                        if ((t0m >> r) & 1u) y = *reinterpret_cast<const float4*>(tile + r * kWinCols + c4);
-                        if ((t1m >> r) & 1u) {
-                            const float4 z = *reinterpret_cast<const float4*>(tile + (BR + r) * kWinCols + c4);
-                            y.x += z.x;
-                            y.y += z.y;
-                            y.z += z.z;
-                            y.w += z.w;
-                        }
-                        *reinterpret_cast<float4*>(part + r * kWinCols + c4) = y;
-                    }
-                    __threadfence();
-                    __syncwarp();
-                    int last = 0;
-                    if (lane == 0) {
-                        const int old = atomicAdd(a.counters + (int64_t)hh * BT + bt, 1);
-                        last = (old == npieces - 1);
-                        if (last) a.counters[(int64_t)hh * BT + bt] = 0;   // ready for the next call
-                    }
-                    last = __shfl_sync(0xffffffffu, last, 0);
-                    if (last) {
-                        __threadfence();
-                        for (int r = h; r < nr; r += 2) {
-                            float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
-                            for (int32_t q = 0; q < npieces; ++q) {
-                                const float* pp =
-                                    a.partial + ((int64_t)(f0 + q) * BT + bt) * BR * kWinCols + r * kWinCols + c4;
-                                const float4 z = __ldcg(reinterpret_cast<const float4*>(pp));
-                                y.x += z.x;
-                                y.y += z.y;
-                                y.z += z.z;
-                                y.w += z.w;
-                            }
-                            if (lane_ok)
-                                *reinterpret_cast<float4*>(a.Y + (b * a.rows + row0 + r) * (int64_t)a.K + col_base) = y;
-                        }
-                    }
+                if (lane == 0) {
+                    rstart[9] = (int32_t)row0;
+                    rstart[10] = nr;
+                    rstart[11] = (int32_t)p;
                 }
-            }
-        } else {
-            // ---- light stripes of the window ----------------------------------------
-            const int64_t s_first = (w - npg) * SPW;
-            for (int64_t s = s_first + warp; s < s_first + SPW && s < a.nstripes; s += kWinWarps) {
+            } else {
+                const int64_t s = (w - npg) * SPW + it;
+                if (s >= a.nstripes) continue;
                 const int64_t row0 = s * BR;
                 const int nr = (int)(row0 + BR < a.rows ? BR : a.rows - row0);
+#if GL_WIN_PREFETCH_INFO
+                if (info[SPW + 1 + it] >= 0) continue;   // heavy: done as pieces
+                b0 = info[it];
+                b1 = info[it + 1];
+                const int32_t* rp = info + 2 * SPW + 1 + it * BR;   // rem_ptr of the stripe's rows
+                j0 = rp[0];
+                j1 = rp[nr];
+                if (lane <= BR) rstart[lane] = lane <= nr ? rp[lane] : j1;
+#else
                 const int32_t hv = a.heavy_of != nullptr ? a.heavy_of[s] : -1;
-                const int32_t b0 = a.stripe_ptr[s], b1 = a.stripe_ptr[s + 1];
-                int32_t rp = 0;
-                if (lane <= nr) rp = a.rem_ptr[row0 + lane];
-                if (hv >= 0) continue;   // done as pieces
-                const int32_t j0 = __shfl_sync(0xffffffffu, rp, 0);
-                const int32_t j1 = __shfl_sync(0xffffffffu, rp, nr);
-                if (lane <= BR) rstart[lane] = lane <= nr ? rp : j1;
-                __syncwarp();
-                uint32_t touched = 0;
-                if (!win_unit<BR>(a, b0, b1, j0, j1, rstart, xb, xw, Xg, lst, tile, touched, lane)) {
-                    if (lane == 0) atomicExch(err, GL_ERR_INVALID_ARGUMENT);
-                    continue;
+                b0 = a.stripe_ptr[s];
+                b1 = a.stripe_ptr[s + 1];
+                int32_t rpl = 0;
+                if (lane <= nr) rpl = a.rem_ptr[row0 + lane];
+                if (hv >= 0) continue;
+                j0 = __shfl_sync(0xffffffffu, rpl, 0);
+                j1 = __shfl_sync(0xffffffffu, rpl, nr);
+                if (lane <= BR) rstart[lane] = lane <= nr ? rpl : j1;
+#endif
+                if (lane == 0) {
+                    rstart[9] = (int32_t)row0;
+                    rstart[10] = nr;
+                    rstart[11] = -1;
                 }
-                const uint32_t t0m = __shfl_sync(0xffffffffu, touched, 0);
-                const uint32_t t1m = __shfl_sync(0xffffffffu, touched, 16);
+            }
+            __syncwarp();
+            uint32_t touched = 0;
+            if (!win_unit<BR>(a, b0, b1, j0, j1, rstart, xb, xw, Xg, lst, tile, touched, lane)) {
+                if (lane == 0) atomicExch(err, GL_ERR_INVALID_ARGUMENT);
+                continue;
+            }
+            const uint32_t t0m = __shfl_sync(0xffffffffu, touched, 0);
+            const uint32_t t1m = __shfl_sync(0xffffffffu, touched, 16);
+            const int64_t row0 = rstart[9];
+            const int nr = rstart[10];
+            const int64_t p = rstart[11];
+            if (p < 0) {
                 if (lane_ok) {
+                    for (int r = h; r < nr; r += 2)
+                        *reinterpret_cast<float4*>(a.Y + ((int64_t)b * a.rows + row0 + r) * (int64_t)a.K +
+                                                   col_base) = win_row<BR>(tile, r, c4, t0m, t1m);
+                }
+            } else {
+                // partial tile -> workspace; the last piece of the stripe reduces
+                float* part = a.partial + (p * BT + bt) * BR * kWinCols;
+                for (int r = h; r < BR; r += 2)
+                    *reinterpret_cast<float4*>(part + r * kWinCols + c4) = win_row<BR>(tile, r, c4, t0m, t1m);
+                __threadfence();
+                __syncwarp();
+                const int32_t hh = a.piece_heavy[p];
+                const int32_t f0 = a.heavy_first[hh];
+                const int32_t npieces = a.heavy_first[hh + 1] - f0;
+                int last = 0;
+                if (lane == 0) {
+                    const int old = atomicAdd(a.counters + (int64_t)hh * BT + bt, 1);
+                    last = (old == npieces - 1);
+                    if (last) a.counters[(int64_t)hh * BT + bt] = 0;   // ready for the next call
+                }
+                last = __shfl_sync(0xffffffffu, last, 0);
+                if (last) {
+                    __threadfence();
                     for (int r = h; r < nr; r += 2) {
                         float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
-                        if ((t0m >> r) & 1u) y = *reinterpret_cast<const float4*>(tile + r * kWinCols + c4);
-                        if ((t1m >> r) & 1u) {
-                            const float4 z = *reinterpret_cast<const float4*>(tile + (BR + r) * kWinCols + c4);
+                        for (int32_t q = 0; q < npieces; ++q) {
+                            const float* pp =
+                                a.partial + ((int64_t)(f0 + q) * BT + bt) * BR * kWinCols + r * kWinCols + c4;
+                            const float4 z = __ldcg(reinterpret_cast<const float4*>(pp));
                             y.x += z.x;
                             y.y += z.y;
                             y.z += z.z;
                             y.w += z.w;
                         }
-                        *reinterpret_cast<float4*>(a.Y + (b * a.rows + row0 + r) * (int64_t)a.K + col_base) = y;
+                        if (lane_ok)
+                            *reinterpret_cast<float4*>(a.Y + ((int64_t)b * a.rows + row0 + r) * (int64_t)a.K +
+                                                       col_base) = y;
                     }
                 }
-                __syncwarp();
             }
+            __syncwarp();
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[buf]);
@@ -574,13 +692,15 @@ __global__ void __launch_bounds__(kWinThreads, 2) window_kernel(const StripeArgs
 // Whether the window kernel serves this SpMM: FP32, whole float4 lanes
 // (K % 4 == 0, 16-byte aligned X / Y), at least one full tile of columns, a
 // workspace (the unit counter lives there), a load-balance schedule with
-// pieces of at most kWinMaxPieceWork entries (so every unit fits a warp's
-// list), and column numbers that fit the list keys.
+// pieces of at most kWinMaxPieceWork entries (so every item fits a warp's
+// list), list keys (float4 index << 3) and unit numbers within 32 bits.
 inline bool window_eligible(const StripeArgs<float>& a) {
     const uintptr_t xa = reinterpret_cast<uintptr_t>(a.X), ya = reinterpret_cast<uintptr_t>(a.Y);
+    const int64_t units = (ceil_div(a.num_pieces, kWinWarps) + ceil_div(a.rows, kWinRows)) * a.batch *
+                          ceil_div(a.K, kWinCols);
     return a.sched != nullptr && a.K >= kWinCols && a.K % 4 == 0 && xa % 16 == 0 && ya % 16 == 0 &&
-           a.piece_work > 0 && a.piece_work <= kWinMaxPieceWork && a.cols < (int64_t(1) << 29) &&
-           a.rows < (int64_t(1) << 31);
+           a.piece_work > 0 && a.piece_work <= kWinMaxPieceWork && a.rows < (int64_t(1) << 31) &&
+           a.cols * (int64_t)(a.K / 4) < (int64_t(1) << 29) && units < (int64_t(1) << 31);
 }
 
 template <int BR>
@@ -599,6 +719,9 @@ int launch_window(const StripeArgs<float>& a0, cudaStream_t stream) {
         occ_cache,
         [&](int* o) {
             GL_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            // two CTAs of ~106 KB need the largest shared-memory carveout
+            GL_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             (int)cudaSharedmemCarveoutMaxShared));
             GL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, kern, kWinThreads, smem));
             return GL_OK;
         },

@@ -168,26 +168,22 @@ def csr_to_pbr(mat, block_rows: int = 2, block_cols: int = 2, min_nnz_per_block:
 
 
 def pbr_to_csr(pbr_mat, indptr, indices, data):
-    """Fill caller-provided CSR arrays from a PBR matrix (``pbr_matrix.cpp:289-338``).
+    """Fill caller-provided CSR arrays from a PBR matrix (``pbr_matrix.cpp:289-338``),
+    computed on the device (``gl_pbr_to_csr``) and copied into the arrays
+    (numpy arrays or torch tensors, any index / value dtype).
 
     Unlike the reference, matrices whose row count is not a multiple of the
     block height are handled (the reference throws ``RuntimeError`` there)."""
-    br, bc = pbr_mat.block_rows, pbr_mat.block_cols
-    codes = np.asarray(pbr_mat.block_codes, dtype=np.uint64)
-    coords = np.asarray(pbr_mat.block_coords, dtype=np.int64).reshape(-1, 2)
-    bits = np.arange(br * bc, dtype=np.uint64)
-    mask = ((codes[:, None] >> bits[None, :]) & np.uint64(1)).astype(bool)
-    blk, bit = np.nonzero(mask)
-    r = np.concatenate([coords[blk, 0] + bit // bc,
-                        np.repeat(np.arange(pbr_mat.rows), np.diff(np.asarray(pbr_mat.remainder_indptr)))])
-    c = np.concatenate([coords[blk, 1] + bit % bc, np.asarray(pbr_mat.remainder_col_ind, dtype=np.int64)])
-    v = np.concatenate([np.asarray(pbr_mat.block_data)[: len(blk)], np.asarray(pbr_mat.remainder_data)])
-    order = np.lexsort((v, c, r))
-    r, c, v = r[order], c[order], v[order]
-    indptr[0] = 0
-    indptr[1:pbr_mat.rows + 1] = np.cumsum(np.bincount(r, minlength=pbr_mat.rows))
-    indices[: len(c)] = c
-    data[: len(v)] = v
+    from ..pbr import device_to_csr
+    dev = _require_cuda("pbr_to_csr")
+    src = pbr_mat._build.codes.device if pbr_mat._build.codes.is_cuda else dev
+    ip, ix, dv = device_to_csr(pbr_mat, src)
+    nnz = ix.numel()
+    for dst, t, n in ((indptr, ip, pbr_mat.rows + 1), (indices, ix, nnz), (data, dv, nnz)):
+        if isinstance(dst, torch.Tensor):
+            dst[:n].copy_(t.to(dst.device, dst.dtype))
+        else:
+            dst[:n] = t.cpu().numpy()
 
 
 def pbr_analyze_csr(mat, block_rows: int = 8, block_cols: int = 8, min_nnz_coverage=1000):

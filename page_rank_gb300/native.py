@@ -128,7 +128,7 @@ class PbrMatrixDesc(_c.Structure):
                 ("num_heavy", _i32), ("num_pieces", _i32), ("piece_work", _i32), ("column_tile", _i32),
                 ("lane_split", _i32),
                 ("heavy_of", _vp), ("heavy_stripe", _vp), ("heavy_first", _vp), ("piece_heavy", _vp),
-                ("kernel", _i32)]
+                ("kernel", _i32), ("piece_range", _vp)]
 
 
 class BuildCounts(_c.Structure):
@@ -169,6 +169,10 @@ _SIGS = {
     "gl_pbr_spmm": (_c.c_int, [_c.POINTER(PbrMatrixDesc), _vp, _vp, _i64, _i64, _vp, _i64, _vp]),
     "gl_pbr_spmm_static": (_c.c_int, [_c.POINTER(PbrMatrixDesc), _vp, _vp, _i64, _i64, _vp]),
     "gl_spmm_workspace_error": (_c.c_int, [_vp, _vp]),
+    "gl_pbr_to_csr_workspace_bytes": (_i64, [_c.POINTER(PbrMatrixDesc)]),
+    "gl_pbr_to_csr": (_c.c_int, [_c.POINTER(PbrMatrixDesc), _vp, _vp, _vp, _vp, _i64, _vp]),
+    "gl_pbr_block_patterns_workspace_bytes": (_i64, [_i64]),
+    "gl_pbr_block_patterns": (_c.c_int, [_vp, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _vp]),
     "gl_ppr_teleport_index": (_c.c_int, [_i64, _i32, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp,
                                          _vp]),
     "gl_ppr_init": (_c.c_int, [_c.POINTER(TeleportDesc), _i64, _i64, _i32, _vp, _vp, _vp, _vp]),

@@ -281,7 +281,7 @@ def pbr_from_device_csr(indptr: torch.Tensor, indices: torch.Tensor, data: torch
 
 
 SCHED_FIELDS = ("num_heavy", "num_pieces", "piece_work", "heavy_of", "heavy_stripe", "heavy_first",
-                "piece_heavy")
+                "piece_heavy", "piece_range")
 
 
 def matrix_desc(meta: dict, rows: int, cols: int, block_rows: int, block_cols: int
@@ -297,6 +297,58 @@ def matrix_desc(meta: dict, rows: int, cols: int, block_rows: int, block_cols: i
         for f in SCHED_FIELDS:
             setattr(d, f, sched[f])
     return d
+
+
+def device_to_csr(pbr: "PBRMatrix", device=None) -> tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
+    """CSR of a PBR matrix computed on the device (``gl_pbr_to_csr``): int32
+    indptr / indices and values of the matrix's value type, rows sorted by
+    column (the reference's ``pbr_to_csr``, ``pbr_matrix.cpp:289-338``)."""
+    from .graph_link import pbr_registry as reg
+
+    dev = torch.device(device) if device is not None else pbr._build.codes.device
+    if dev.type != "cuda":
+        raise RuntimeError("device_to_csr needs a CUDA device")
+    mat = pbr.to(dev)
+    meta = reg.get_pbr_gpu_meta(mat)
+    d = _array_desc(meta, pbr.rows, pbr.cols, pbr.block_rows, pbr.block_cols)
+    L = native.lib()
+    nbytes = int(L.gl_pbr_to_csr_workspace_bytes(d))
+    if nbytes < 0:
+        raise ValueError("matrix too large for an int32 CSR")
+    nnz = int(d.packed_nnz + d.remainder_nnz)
+    with torch.cuda.device(dev):
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        indptr = torch.empty(pbr.rows + 1, dtype=torch.int32, device=dev)
+        indices = torch.empty(nnz, dtype=torch.int32, device=dev)
+        data = torch.empty(nnz, dtype=meta["data"].dtype, device=dev)
+        native.check(L.gl_pbr_to_csr(d, indptr.data_ptr(), _ptr(indices), _ptr(data), ws.data_ptr(), nbytes,
+                                     _stream_handle(dev)))
+    return indptr, indices, data
+
+
+def block_patterns(codes: torch.Tensor, min_nnz_coverage: int) -> tuple[np.ndarray, np.ndarray, dict]:
+    """Distinct block codes (ascending, uint64), their occurrence counts and
+    the coverage-rule totals, counted on the device
+    (``gl_pbr_block_patterns``)."""
+    dev = codes.device
+    nb = int(codes.numel())
+    L = native.lib()
+    nbytes = int(L.gl_pbr_block_patterns_workspace_bytes(nb))
+    if nbytes < 0:
+        raise ValueError("too many blocks")
+    with torch.cuda.device(dev):
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        uniq = torch.empty(max(nb, 1), dtype=torch.int64, device=dev)
+        counts = torch.empty(max(nb, 1), dtype=torch.int64, device=dev)
+        small = torch.zeros(5, dtype=torch.int64, device=dev)    # [num_unique, totals[4]]
+        native.check(L.gl_pbr_block_patterns(_ptr(codes.contiguous()), nb, int(min_nnz_coverage),
+                                             uniq.data_ptr(), counts.data_ptr(), small.data_ptr(),
+                                             small[1:].data_ptr(), ws.data_ptr(), nbytes, _stream_handle(dev)))
+        sm = small.cpu().numpy()
+    u = int(sm[0])
+    totals = {"accounted_nnz": int(sm[1]), "remainder_nnz": int(sm[2]), "accounted_patterns": int(sm[3]),
+              "accounted_blocks": int(sm[4])}
+    return uniq[:u].cpu().numpy().view(np.uint64), counts[:u].cpu().numpy(), totals
 
 
 def validate_arrays(meta: dict, rows: int, cols: int, block_rows: int, block_cols: int) -> None:

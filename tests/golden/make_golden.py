@@ -20,6 +20,12 @@ Writes:
   ``normalize_transition_matrix``, on edge lists with invalid edges,
   duplicates (equal weights, or at most two copies, or short rows), long
   columns and empty graphs;
+* ``pbr_to_csr_cases.npz`` — the reference ``pbr_to_csr``
+  (``Backend/graph_link/pbr_matrix/pbr_matrix.cpp:289-338``) applied to the
+  reference builder's output for every builder case whose row count is a
+  multiple of the block height (the reference throws on the others);
+  ``python tests/golden/make_golden.py --only pbr_to_csr`` writes just this
+  file;
 * ``ppr_nx_cases.npz`` — the NetworkX PPR values the reference's accuracy
   test compares against (``Tests/test_ppr_accuracy.py:14-40``), with the
   column-stochastic matrices they come from, so GPU machines without
@@ -147,10 +153,34 @@ def edge_cases():
     return cases
 
 
+def pbr_to_csr_cases(core):
+    """The reference pbr_to_csr on the reference builder's PBR of each builder
+    case (cases with a ragged last stripe are left out: it throws there)."""
+    out = {}
+    names = []
+    for name, A, br, bc, mn in builder_cases():
+        if A.shape[0] % br != 0:
+            continue
+        p = core.csr_to_pbr(A.indptr, A.indices, A.data, A.shape[0], A.shape[1], br, bc, mn)
+        indptr = np.zeros(A.shape[0] + 1, A.indptr.dtype)
+        indices = np.zeros(A.nnz, A.indices.dtype)
+        data = np.zeros(A.nnz, A.data.dtype)
+        core.pbr_to_csr(p, indptr, indices, data)
+        names.append(name)
+        out[f"{name}/out_indptr"], out[f"{name}/out_indices"], out[f"{name}/out_data"] = indptr, indices, data
+    out["names"] = np.array(names)
+    np.savez_compressed(HERE / "pbr_to_csr_cases.npz", **out)
+
+
 def main():
     core = ref_build.load_reference_core()
     if core is None:
         raise SystemExit("build the reference first: python oracle/ref_build.py")
+    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "pbr_to_csr":
+        pbr_to_csr_cases(core)
+        print("wrote pbr_to_csr_cases.npz")
+        return
+    pbr_to_csr_cases(core)
     out = {}
     names = []
     for name, A, br, bc, mn in builder_cases():

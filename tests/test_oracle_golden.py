@@ -44,6 +44,29 @@ def test_oracle_pbr_expands_to_input():
         assert np.array_equal(vals, A.data), name
 
 
+def _pbr_to_csr_golden():
+    z = np.load(GOLDEN / "pbr_to_csr_cases.npz")
+    return {str(n): (z[f"{n}/out_indptr"], z[f"{n}/out_indices"], z[f"{n}/out_data"]) for n in z["names"]}
+
+
+def test_reference_pbr_to_csr_golden_pinned():
+    """The reference pbr_to_csr's output (golden) is the input CSR of every
+    case it accepts, and the oracle's expansion agrees with it bit for bit."""
+    gold = _pbr_to_csr_golden()
+    assert len(gold) >= 10
+    for name, A, br, bc, mn, ref in CASES:
+        if name not in gold:
+            assert A.shape[0] % br != 0, name     # only ragged cases are left out
+            continue
+        gip, gix, gdv = gold[name]
+        assert np.array_equal(gip, A.indptr) and np.array_equal(gix, A.indices), name
+        assert np.array_equal(gdv.view(np.uint8), A.data.view(np.uint8)), name
+        pbr = dict(ref, rows=A.shape[0], cols=A.shape[1], block_rows=br, block_cols=bc)
+        indptr, indices, vals = oracle.pbr_to_csr(pbr)
+        assert np.array_equal(indptr, gip.astype(indptr.dtype)) and np.array_equal(indices, gix), name
+        assert np.array_equal(vals, gdv), name
+
+
 def test_bucket_chain_shape():
     ch = oracle.bucket_chain(362, 5000)
     assert ch[0, 0] == 0 and ch[0, 1] >= 362
