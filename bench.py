@@ -66,18 +66,20 @@ def measured_peak():
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def profile_traffic(log2n: int, features: int):
-    """DRAM bytes per launch from the committed ncu summary of this workload
-    (captured for n = 2^20 and 64 columns only; None for other sizes)."""
-    p = ROOT / "profiles" / "stripe_kernel_spmm_rmat2e20_64cols.md"
-    if log2n != 20 or features != 64 or not p.is_file():
+def profile_traffic(log2n: int, features: int, kernel: str):
+    """DRAM bytes per launch of this workload's kernel from the committed
+    one-pass ncu capture (profiles/dram_traffic.json; None when that size /
+    kernel was not captured)."""
+    p = ROOT / "profiles" / "dram_traffic.json"
+    if not p.is_file():
         return None
-    for line in p.read_text().splitlines():
-        if line.startswith("dram_bytes_per_launch:"):
-            try:
-                return int(float(line.split(":", 1)[1].strip()))
-            except ValueError:
-                return None
+    try:
+        entries = json.loads(p.read_text())["captures"]
+    except (ValueError, KeyError):
+        return None
+    for e in entries:
+        if e.get("log2n") == log2n and e.get("features") == features and e.get("kernel") == kernel:
+            return int(e["dram_bytes_per_launch"])
     return None
 
 
@@ -289,7 +291,7 @@ def run_ours(args, rank, world, local_rank):
     out = None
     if rank == 0:
         peak, peak_kind = measured_peak()
-        traffic = profile_traffic(args.log2n, F)
+        traffic = profile_traffic(args.log2n, F, "stripe_kernel")
         out = {
             "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 5),
@@ -394,7 +396,7 @@ def run_ppr(dev, args) -> dict:
     from page_rank_gb300 import synth
     from page_rank_gb300.autotune import autotune
     from page_rank_gb300.engine import PPREngine
-    from page_rank_gb300.warmstart import WarmStart
+    from page_rank_gb300.warmstart import WarmStart, WarmStartGate
 
     K = 256
     t0 = time.perf_counter()
@@ -418,18 +420,27 @@ def run_ppr(dev, args) -> dict:
     eng.solve_plain(sets[:2], alpha=PPR_ALPHA, tol=PPR_TOL)
     rp = eng.solve_plain(sets[:plain_n], alpha=PPR_ALPHA, tol=PPR_TOL)
     sampler.stop()
-    # warm start: the network trained on plain-method vectors of this graph
-    ws = WarmStart(eng, seed=0)
+    # warm start: the network trained on plain-method vectors of this graph,
+    # used as configured (its gate predicts only when the estimated saving
+    # beats the prediction's cost; the first batch calibrates it) and forced
+    # on every column
+    ws = WarmStart(eng, seed=0, gate=WarmStartGate())
     t0 = time.perf_counter()
     stats = ws.train(num_vectors=args.ppr_train_vectors, batch=256, nodes_per_vector=512, epochs=3)
     train_s = time.perf_counter() - t0
-    ws.solve(sets[:8], alpha=PPR_ALPHA, tol=PPR_TOL)
+    ws.solve(sets[:8], alpha=PPR_ALPHA, tol=PPR_TOL)         # warm-up and the gate's first measurement
     torch.cuda.synchronize(dev)
     rw = ws.solve(sets, alpha=PPR_ALPHA, tol=PPR_TOL, retire=True, use_graphs=True)
+    gate = ws.gate.summary()
+    forced = WarmStart(eng, seed=0)
+    forced.mlp = ws.mlp
+    rf = forced.solve(sets, alpha=PPR_ALPHA, tol=PPR_TOL, retire=True, use_graphs=True)
     qps_b = K / rb.seconds
     qps_p = plain_n / rp.seconds
     qps_w = K / rw.seconds
-    same = float((rb.X.double() - rw.X.double()).abs().sum(dim=0).max().item())
+    qps_f = K / rf.seconds
+    same = float(max((rb.X.double() - rw.X.double()).abs().sum(dim=0).max().item(),
+                     (rb.X.double() - rf.X.double()).abs().sum(dim=0).max().item()))
     out = {
         "workload": f"batched PPR: {g.description}; {K} seed sets of 1-32 uniform seeds, alpha {PPR_ALPHA}, "
                     f"per-column L1 {PPR_TOL:g} to the fixed point (certified stop), retirement + CUDA graphs",
@@ -443,11 +454,15 @@ def run_ppr(dev, args) -> dict:
         "batched_warm": {"queries_per_s": round(qps_w, 2), "seconds_including_prediction": round(rw.seconds, 4),
                          "iterations_sum": int(rw.iterations.sum()), "column_steps": rw.column_steps,
                          "columns_using_prediction": float(np.mean(rw.warm_columns)),
-                         "train_vectors": stats.vectors, "train_s": round(train_s, 2),
+                         "gate": gate, "train_vectors": stats.vectors, "train_s": round(train_s, 2),
                          "all_converged": bool(rw.converged.all())},
+        "batched_warm_forced": {"queries_per_s": round(qps_f, 2), "seconds_including_prediction": round(rf.seconds, 4),
+                                "iterations_sum": int(rf.iterations.sum()),
+                                "columns_using_prediction": float(np.mean(rf.warm_columns)),
+                                "all_converged": bool(rf.converged.all())},
         "speedup_batched_vs_plain": round(qps_b / qps_p, 2),
         "speedup_batched_warm_vs_plain": round(qps_w / qps_p, 2),
-        "iterations_cold_over_warm": round(float(rb.iterations.sum()) / max(1, int(rw.iterations.sum())), 3),
+        "iterations_cold_over_warm_forced": round(float(rb.iterations.sum()) / max(1, int(rf.iterations.sum())), 3),
         "max_l1_cold_vs_warm": same,
         "clocks": clocks,
     }
@@ -456,7 +471,7 @@ def run_ppr(dev, args) -> dict:
         sample = list(range(min(cores, K)))
         cpu = cpu_ppr_leg(g, [sets[i] for i in sample], cores)
         Xg = rb.X[:, torch.tensor(sample, device=dev)].double().cpu().numpy()
-        Xw = rw.X[:, torch.tensor(sample, device=dev)].double().cpu().numpy()
+        Xw = rf.X[:, torch.tensor(sample, device=dev)].double().cpu().numpy()
         d_b = np.abs(Xg - cpu["X"]).sum(axis=0) + cpu["bound"]
         d_w = np.abs(Xw - cpu["X"]).sum(axis=0) + cpu["bound"]
         out["parity"] = {"max_l1_vs_fp64": float(d_b.max()), "max_l1_warm_vs_fp64": float(d_w.max()),

@@ -360,7 +360,10 @@ int gl_ppr_dangling_mass(const void* X, int64_t rows, int64_t K, int32_t value_t
  * residual_hist and row t + 1 of dangling_hist and reads row t of
  * dangling_hist.  A step is a no-op when t >= max_iterations, or (STOP_ALL)
  * when max_k residual_hist[t-1][k] < tol.  Under STOP_PER_COLUMN, a column
- * whose residual_hist[t-1][k] < tol is copied unchanged and adds 0.
+ * whose residual_hist[t-1][k] < tol is copied unchanged and adds 0; a column
+ * tile whose columns all stopped is not recomputed (copied once, then left
+ * as both iterate buffers already hold it), and the dangling entries of
+ * stopped columns are not accumulated.
  * workspace: as for gl_pbr_spmm with batch 1 and K features.
  */
 typedef struct gl_ppr_step_params {

@@ -44,6 +44,8 @@
 namespace gl {
 
 constexpr int kStripeThreads = 256;
+constexpr int kWinDrawRows = 64;   // rows per window of the window draw
+constexpr int kWinDrawRing = 16;   // windows a CTA can have in flight
 
 constexpr int kStripeWarps = kStripeThreads / 32;
 
@@ -117,6 +119,7 @@ struct StripeArgs {
     int32_t cta_sums;              // 1: per-column sums gathered per CTA in shared memory (2 * K doubles
                                    //    after the stripe buffers), one global atomic per CTA and column
     int32_t variant;               // gl_pbr_matrix.kernel: 0 automatic, 1 stripe kernel, 2 window kernel
+    int32_t win_draw;              // 1: light stripes drawn window by window (needs sched)
 };
 
 template <typename S, int V>
@@ -132,6 +135,34 @@ __device__ __forceinline__ Pack<S, V> load_pack_cg(const S* p) {
 }
 template <typename S, int V>
 __device__ __forceinline__ void store_pack(S* p, const Pack<S, V>& v) {
+    *reinterpret_cast<Pack<S, V>*>(p) = v;
+}
+
+// Store of a finished output row (Y, or X_out of a power-iteration step):
+// with GL_Y_EVICT_FIRST the row is marked first to leave L2 (it is not read
+// again by this launch), keeping more of the gathered X rows resident.
+#ifndef GL_Y_EVICT_FIRST
+#define GL_Y_EVICT_FIRST 0
+#endif
+template <typename S, int V>
+__device__ __forceinline__ void store_out(S* p, const Pack<S, V>& v) {
+#if GL_Y_EVICT_FIRST
+    if constexpr (sizeof(S) == 4 && V == 4) {
+        unsigned long long pol;
+        asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+        asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "f"(v.v[0]),
+                     "f"(v.v[1]), "f"(v.v[2]), "f"(v.v[3]), "l"(pol)
+                     : "memory");
+        return;
+    } else if constexpr (sizeof(S) == 4 && V == 2) {
+        unsigned long long pol;
+        asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+        asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.v[0]), "f"(v.v[1]),
+                     "l"(pol)
+                     : "memory");
+        return;
+    }
+#endif
     *reinterpret_cast<Pack<S, V>*>(p) = v;
 }
 
@@ -768,6 +799,10 @@ stripe_kernel(const StripeArgs<S> a) {
     using SM = StripeSmem<S, BR, V, C>;
     extern __shared__ __align__(16) unsigned char xs_dyn[];
     __shared__ int s_skip;
+    // window draw: stripes handed out to this CTA's warps, and the ring of
+    // the CTA's drawn windows ((sequence << 32) | window)
+    __shared__ unsigned int s_take;
+    __shared__ unsigned long long s_ring[kWinDrawRing];
     const int warp = threadIdx.x >> 5;
     S* const otile = reinterpret_cast<S*>(xs_dyn) + (size_t)warp * BR * T;
     Entry<S>* const lst = reinterpret_cast<Entry<S>*>(xs_dyn + SM::tile) + (size_t)warp * kListCap;
@@ -840,10 +875,77 @@ stripe_kernel(const StripeArgs<S> a) {
     };
 
     // next work item: drawn from the counter, or static round-robin
+    // Window draw: the heavy-stripe pieces are drawn one at a time from the
+    // global counter (tile by tile); then the CTA works through 64-row
+    // windows of light stripes (for one column tile each), its warps taking the
+    // window's stripes in turn, so the X rows of the window's diagonal block
+    // (most of its nonzeros on locality-ordered graphs) are gathered by
+    // warps of one CTA close together in time and hit its L1.  The warp that
+    // takes a window's first stripe draws the window from a second global
+    // counter and publishes it in the ring; the others wait for it (bounded).
+#ifndef GL_TILE_MAJOR_SPMM
+#define GL_TILE_MAJOR_SPMM 0
+#endif
+    constexpr bool tile_major_items = PPR || GL_TILE_MAJOR_SPMM;
+    constexpr int SPW = kWinDrawRows / BR;
+    const int64_t nwin = (a.nstripes + SPW - 1) / SPW;
+    bool phase_windows = false;
+    if (a.win_draw) {
+        if (threadIdx.x == 0) s_take = 0;
+        if (threadIdx.x < kWinDrawRing) s_ring[threadIdx.x] = ~0ull;
+        __syncthreads();
+    }
     auto next_item = [&](int64_t cur) -> int64_t {
         if (a.sched == nullptr) return cur + nwarps;
         unsigned long long v = 0;
-        if (lane == 0) v = atomicAdd(a.sched, 1ull);
+        if (!a.win_draw) {
+            if (lane == 0) v = atomicAdd(a.sched, 1ull);
+            return (int64_t)__shfl_sync(0xffffffffu, v, 0);
+        }
+        // item number of (unit, batch x tile) in this launch's numbering
+        auto item_of = [&](int64_t unit, int64_t btile) -> unsigned long long {
+            return (unsigned long long)(tile_major_items ? btile * units + unit : unit * BT + btile);
+        };
+        if (lane == 0) {
+            v = items;   // done unless a unit is found
+            if (!phase_windows) {
+                const unsigned long long p = atomicAdd(a.sched, 1ull);
+                if ((int64_t)p < (int64_t)a.num_pieces * BT) {
+                    v = item_of((int64_t)p % a.num_pieces, (int64_t)p / a.num_pieces);   // pieces tile by tile
+                } else {
+                    phase_windows = true;
+                }
+            }
+            while (phase_windows) {
+                const unsigned int tk = atomicAdd(&s_take, 1u);
+                const unsigned int wl = tk / SPW, j = tk % SPW;
+                volatile unsigned long long* slot = &s_ring[wl % kWinDrawRing];
+                unsigned long long w;
+                if (j == 0) {
+                    w = atomicAdd(a.sched + 3, 1ull);
+                    *slot = ((unsigned long long)wl << 32) | (w & 0xffffffffull);
+                } else {
+                    const long long t0 = clock64();
+                    unsigned long long e = *slot;
+                    while ((e >> 32) != wl) {
+                        if (clock64() - t0 > 4000000000LL) {   // about two seconds: record and stop
+                            atomicExch(reinterpret_cast<int*>(a.sched + 2), GL_ERR_TIMEOUT);
+                            e = ((unsigned long long)wl << 32) | 0xffffffffull;
+                            break;
+                        }
+                        e = *slot;
+                    }
+                    w = e & 0xffffffffull;
+                }
+                if ((int64_t)w >= nwin * BT) break;                  // no windows left: done
+                const int64_t st = ((int64_t)w % nwin) * SPW + j;     // windows tile by tile
+                if (st < a.nstripes) {
+                    v = item_of(a.num_pieces + st, (int64_t)w / nwin);
+                    break;
+                }
+                // past the last stripe of the last window: take again
+            }
+        }
         return (int64_t)__shfl_sync(0xffffffffu, v, 0);
     };
     for (int64_t item = a.sched != nullptr ? next_item(0) : warp_id; item < items; item = next_item(item)) {
@@ -852,16 +954,53 @@ stripe_kernel(const StripeArgs<S> a) {
         // residual sums are flushed (atomically) a few times per launch, not
         // at nearly every item; the SpMM keeps a unit's tiles adjacent (the
         // second decode of a stripe finds its matrix data in L2)
-#ifndef GL_TILE_MAJOR_SPMM
-#define GL_TILE_MAJOR_SPMM 0
-#endif
-        constexpr bool tile_major = PPR || GL_TILE_MAJOR_SPMM;
+        constexpr bool tile_major = tile_major_items;
         const int64_t u = tile_major ? item % units : item / BT;
         const int64_t bt = tile_major ? item / units : item - u * BT;
         const int64_t b = bt / a.ntiles;
         const int tile = (int)(bt - b * a.ntiles);
         const int col_base = tile * T + c_lane * V;
         const bool lane_ok = col_base < a.K;
+
+        if constexpr (PPR) {
+            // STOP_PER_COLUMN: a tile whose columns all stopped is not
+            // recomputed.  Columns frozen at this step (residual of step t-1
+            // below their threshold) are copied X_in -> X_out; once a column
+            // was also frozen at the step before, both iterate buffers hold
+            // its final values and the tile is skipped outright.
+            if (a.stop_mode == GL_PPR_STOP_PER_COLUMN && t >= 1) {
+                bool fz = true, st = true;
+                if (lane_ok) {
+#pragma unroll
+                    for (int j = 0; j < V; ++j) {
+                        const int col = col_base + j;
+                        const double tl = a.col_tol != nullptr ? a.col_tol[col] : a.tol;
+                        fz = fz && a.res_hist[(int64_t)(t - 1) * a.K + col] < tl;
+                        st = st && t >= 2 && a.res_hist[(int64_t)(t - 2) * a.K + col] < tl;
+                    }
+                }
+                const bool all_frozen = __all_sync(0xffffffffu, fz);
+                if (all_frozen && __all_sync(0xffffffffu, st && fz)) continue;
+                if (all_frozen) {
+                    int64_t s_copy = -1;
+                    if (u < a.num_pieces) {
+                        const int32_t hc = a.piece_heavy[u];
+                        if (u == a.heavy_first[hc]) s_copy = a.heavy_stripe[hc];   // the stripe's first piece copies
+                    } else {
+                        s_copy = u - a.num_pieces;
+                        if (a.heavy_of != nullptr && a.heavy_of[s_copy] >= 0) s_copy = -1;   // done as pieces
+                    }
+                    if (s_copy >= 0 && lane_ok && p_lane == 0) {
+                        for (int r = 0; r < BR; ++r) {
+                            const int64_t row = s_copy * BR + r;
+                            if (row < a.rows)
+                                store_pack<S, V>(a.Y + row * a.K + col_base, load_pack<S, V>(a.X + row * a.K + col_base));
+                        }
+                    }
+                    continue;
+                }
+            }
+        }
 
         // ---- the unit: a light stripe or one piece of a heavy stripe -------
         int64_t s;
@@ -976,7 +1115,7 @@ stripe_kernel(const StripeArgs<S> a) {
 #pragma unroll 2
                 for (int r = 0; r < BR; ++r) {
                     const int64_t row = s * BR + r;
-                    if (row < a.rows) store_pack<S, V>(Yb + row * a.K, load_pack<S, V>(trow + r * T));
+                    if (row < a.rows) store_out<S, V>(Yb + row * a.K, load_pack<S, V>(trow + r * T));
                 }
             } else {
                 // this step's per-column terms (computed here, not kept in
@@ -1024,7 +1163,7 @@ stripe_kernel(const StripeArgs<S> a) {
                             res_acc[j] += (float)fabs(nv - old.v[j]);
                             if (dang) dang_acc[j] += (float)nv;
                         }
-                        store_pack<S, V>(Xout + row * a.K, o);
+                        store_out<S, V>(Xout + row * a.K, o);
                     }
                 }
             }
@@ -1048,6 +1187,7 @@ stripe_kernel(const StripeArgs<S> a) {
         if (atomicAdd(a.sched + 1, 1ull) == (unsigned long long)nwarps - 1) {
             a.sched[0] = 0;
             a.sched[1] = 0;
+            a.sched[3] = 0;
             __threadfence();
         }
     }

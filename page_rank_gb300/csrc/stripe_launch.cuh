@@ -20,6 +20,12 @@ int launch_stripe_shape(const StripeArgs<S>& a0, cudaStream_t stream) {
     // per-column sums per CTA (2 * K doubles of shared memory)
     constexpr int64_t kCtaSumCols = 512;
     a.cta_sums = (PPR && a.K <= kCtaSumCols) ? 1 : 0;
+#ifndef GL_WINDOW_DRAW
+#define GL_WINDOW_DRAW 1
+#endif
+    // light stripes are drawn window by window (L1 reuse of the diagonal
+    // block's X rows within a CTA)
+    a.win_draw = (GL_WINDOW_DRAW && a.sched != nullptr) ? 1 : 0;
     const size_t smem = base + (a.cta_sums ? (size_t)(2 * a.K) * sizeof(double) : 0);
     // the shared-memory attribute is per device, so it is set (and the
     // occupancy measured) once for every device that launches this instance

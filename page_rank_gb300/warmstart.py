@@ -16,6 +16,15 @@ to the same tolerance, so the fixed point and its accuracy do not depend on
 the network.  A column whose first-step residual from the predicted start is
 larger than from the cold start (the teleport vector) falls back to the cold
 start.
+
+:class:`WarmStartGate` decides per batch whether predicting is worth it: each
+prediction measures its own cost (seconds per column) and, from the two
+first-step residuals, the iterations it saves (the error shrinks about
+geometrically, so a start whose residual is r_warm instead of r_cold saves
+log(r_cold / r_warm) / log(1 / rate) iterations); a fused step of the same
+batch gives the cost of one iteration per column.  Later batches predict
+only while the estimated saving exceeds the cost, with a probe every
+``probe_every`` batches to follow changes.
 """
 from __future__ import annotations
 
@@ -110,11 +119,55 @@ class TrainStats:
     losses: list = field(default_factory=list)
 
 
+class WarmStartGate:
+    """Cost / benefit record of the warm start's predictions (see the module
+    docstring).  Exponential moving averages; ``rate`` is the assumed
+    per-iteration contraction of the error (the damping factor bounds it)."""
+
+    def __init__(self, probe_every: int = 16, rate: float = 0.85, smoothing: float = 0.5):
+        self.probe_every = int(probe_every)
+        self.rate = float(rate)
+        self.smoothing = float(smoothing)
+        self.pred_s_per_col: float | None = None     # prediction seconds per column
+        self.saved_iters: float | None = None        # estimated iterations saved per column
+        self.iter_s_per_col: float | None = None     # seconds of one iteration per column
+        self.calls = 0
+        self.predictions = 0
+
+    def _ema(self, old, new):
+        return new if old is None else self.smoothing * old + (1.0 - self.smoothing) * new
+
+    def want_prediction(self) -> bool:
+        self.calls += 1
+        if None in (self.pred_s_per_col, self.saved_iters, self.iter_s_per_col):
+            return True
+        if self.probe_every > 0 and self.calls % self.probe_every == 0:
+            return True
+        return self.saved_iters * self.iter_s_per_col > self.pred_s_per_col
+
+    def record(self, pred_seconds: float, step_seconds: float, columns: int, r_warm: np.ndarray,
+               r_cold: np.ndarray) -> None:
+        k = max(1, int(columns))
+        ratio = np.maximum(np.asarray(r_cold, np.float64), 1e-300) / np.maximum(np.asarray(r_warm, np.float64),
+                                                                               1e-300)
+        saved = np.where(ratio > 1.0, np.log(ratio) / math.log(1.0 / self.rate), 0.0)
+        self.pred_s_per_col = self._ema(self.pred_s_per_col, pred_seconds / k)
+        self.iter_s_per_col = self._ema(self.iter_s_per_col, step_seconds / k)
+        self.saved_iters = self._ema(self.saved_iters, float(saved.mean()))
+        self.predictions += 1
+
+    def summary(self) -> dict:
+        return {"predictions": self.predictions, "batches": self.calls,
+                "prediction_s_per_column": self.pred_s_per_col, "saved_iterations_per_column": self.saved_iters,
+                "iteration_s_per_column": self.iter_s_per_col}
+
+
 class WarmStart:
     """Feature extraction, training and warm-started solves for one engine."""
 
-    def __init__(self, engine: PPREngine, seed: int = 0):
+    def __init__(self, engine: PPREngine, seed: int = 0, gate: WarmStartGate | None = None):
         self.eng = engine
+        self.gate = gate
         self.dev = engine.device
         self.mlp = MLP(self.dev, seed)
         n = engine.n
@@ -240,11 +293,26 @@ class WarmStart:
 
     def start_vectors(self, seed_sets, alpha) -> tuple[torch.Tensor, np.ndarray]:
         """Start columns: the prediction where its first residual is below the
-        cold start's, else the teleport vector; and which columns use it."""
+        cold start's, else the teleport vector; and which columns use it.
+        With a gate that finds the prediction not worth its cost, every
+        column starts cold and nothing is predicted."""
+        if self.gate is not None and not self.gate.want_prediction():
+            return self.seed_matrix(seed_sets), np.zeros(len(seed_sets), dtype=bool)
+        timed = self.gate is not None
+        if timed:
+            torch.cuda.synchronize(self.dev)
+        t0 = time.perf_counter()
         x_warm = self.predict(seed_sets)
+        if timed:
+            torch.cuda.synchronize(self.dev)
+        t1 = time.perf_counter()
         V = self.seed_matrix(seed_sets)
         r_warm = self.first_residual(seed_sets, x_warm, alpha)
-        r_cold = self.first_residual(seed_sets, V, alpha)
+        if timed:
+            r_cold, step_s = self.first_residual(seed_sets, V, alpha, timing=True)
+            self.gate.record(t1 - t0, step_s, len(seed_sets), r_warm, r_cold)
+        else:
+            r_cold = self.first_residual(seed_sets, V, alpha)
         use_warm = r_warm < r_cold
         return torch.where(torch.from_numpy(use_warm).to(self.dev)[None, :], x_warm, V), use_warm
 
@@ -252,12 +320,20 @@ class WarmStart:
         """Warm-started batched solve with per-column fallback to the cold start."""
         return self.eng.solve(seed_sets, alpha=alpha, tol=tol, max_iterations=max_iterations, warm_start=self, **kw)
 
-    def first_residual(self, seed_sets, x0: torch.Tensor, alpha: float) -> np.ndarray:
-        """||P(x0) - x0||_1 per column (one fused step)."""
+    def first_residual(self, seed_sets, x0: torch.Tensor, alpha: float, timing: bool = False):
+        """||P(x0) - x0||_1 per column (one fused step); with ``timing`` also
+        the seconds of one fused step over these columns (CUDA events)."""
         ptr, rows, w = self.eng.teleport(seed_sets)
         tp = teleport_from_seed_sets(ptr, rows, self.eng.n, self.eng.block_size, w)
         run = PprRun(self.eng.meta, self.eng.n, self.eng.n, self.eng.block_size, self.eng.block_size, tp,
                      alpha, 2, 0.0, native.GL_PPR_STOP_ALL, self.eng.dbits)
         run.init(x0)
+        if not timing:
+            run.launch_chunk(2)
+            return run.res_hist[0].cpu().numpy()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
         run.launch_chunk(2)
-        return run.res_hist[0].cpu().numpy()
+        e1.record()
+        res = run.res_hist[0].cpu().numpy()
+        return res, e0.elapsed_time(e1) / 2e3

@@ -135,7 +135,7 @@ def serving_pass(device, rates=(200.0, 800.0, 3200.0), requests_per_rate: int = 
     Poisson arrivals at each rate, 1-64 seeds per request, alpha in
     {0.8, 0.85, 0.9}, certified L1 1e-6; p50 / p99 latency and queries/s."""
     from .serving import PPRServer, latency_summary
-    from .warmstart import WarmStart
+    from .warmstart import WarmStart, WarmStartGate
     rng = np.random.default_rng(seed)
     sizes = np.sort(np.round(rng.uniform(16, 22, graphs)).astype(int))
     srv = PPRServer(device=device, chunk=8)
@@ -150,8 +150,10 @@ def serving_pass(device, rates=(200.0, 800.0, 3200.0), requests_per_rate: int = 
         g = synth.cluster_zipf_graph(log2n=int(lg), mean_degree=20.0, seed=200 + i, device=device)
         eng = srv.add_graph(f"g{i}", g.A, dangling=g.dangling, block_size=8, min_nnz=4)
         if ws_model is not None:
-            w = WarmStart(eng, seed=0)
-            w.mlp = ws_model.mlp          # one model for the whole graph class
+            # one model for the whole graph class; each graph's gate keeps the
+            # prediction only where it saves more than it costs
+            w = WarmStart(eng, seed=0, gate=WarmStartGate())
+            w.mlp = ws_model.mlp
             srv.warm[f"g{i}"] = w
         descr.append(int(g.n))
     # warm up every graph once
@@ -184,6 +186,8 @@ def serving_pass(device, rates=(200.0, 800.0, 3200.0), requests_per_rate: int = 
     finally:
         srv.stop()
     out["admission_waits"] = srv.admission_waits
+    if warm:
+        out["warm_gates"] = {name: w.gate.summary() for name, w in srv.warm.items() if w.gate is not None}
     return out
 
 

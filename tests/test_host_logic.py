@@ -110,3 +110,28 @@ def test_dangling_bitmap_matches_host_packing():
         m = rng.random(n) < 0.5
         m[-1] = True
         assert torch.equal(dangling_bitmap(torch.from_numpy(m)), _bitmap_from_mask(m, "cpu"))
+
+
+def test_warm_start_gate_keeps_prediction_only_when_it_pays():
+    """The gate predicts until it has a measurement, then only while the
+    estimated saving (iterations x seconds per column-iteration) beats the
+    prediction's cost, probing again every probe_every batches."""
+    import numpy as np
+    from page_rank_gb300.warmstart import WarmStartGate
+    g = WarmStartGate(probe_every=4, rate=0.5, smoothing=0.0)
+    assert g.want_prediction()                                   # nothing measured yet
+    # residual 8x smaller: log(8) / log(2) = 3 iterations saved per column,
+    # each worth 1 ms per column, against 5 ms of prediction per column
+    g.record(pred_seconds=0.010, step_seconds=0.002, columns=2, r_warm=np.array([1.0, 1.0]),
+             r_cold=np.array([8.0, 8.0]))
+    assert abs(g.saved_iters - 3.0) < 1e-12
+    decisions = [g.want_prediction() for _ in range(6)]          # calls 2..7: only call 4 probes
+    assert decisions == [False, False, True, False, False, False]
+    # a cheap prediction pays: 3 x 1 ms > 0.5 ms
+    g.record(pred_seconds=0.001, step_seconds=0.002, columns=2, r_warm=np.array([1.0, 1.0]),
+             r_cold=np.array([8.0, 8.0]))
+    assert g.want_prediction()
+    # a start that is no better than the cold one saves nothing
+    g2 = WarmStartGate(smoothing=0.0)
+    g2.record(0.001, 0.002, 1, np.array([2.0]), np.array([1.0]))
+    assert g2.saved_iters == 0.0 and not g2.want_prediction()
