@@ -216,6 +216,9 @@ def run_ours(args, rank, world, local_rank):
     gen.manual_seed(1234 + rank)
     X = torch.rand((n, F), generator=gen, device=dev, dtype=torch.float32)
     Y = torch.empty((n, F), device=dev, dtype=torch.float32)
+    # the kernel choice rides in the matrix's metadata, so the end-to-end
+    # arm (which builds its own descriptor) runs the same kernel
+    meta["kernel"] = {"auto": 0, "stripe": 1, "window": 2}[args.kernel]
     desc = matrix_desc(meta, n, n, 8, 8)
     L = native.lib()
     stream = torch.cuda.current_stream(dev)
@@ -291,7 +294,7 @@ def run_ours(args, rank, world, local_rank):
     out = None
     if rank == 0:
         peak, peak_kind = measured_peak()
-        traffic = profile_traffic(args.log2n, F, "stripe_kernel")
+        traffic = profile_traffic(args.log2n, F, "window_kernel" if args.kernel == "window" else "stripe_kernel")
         out = {
             "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 5),
@@ -305,7 +308,10 @@ def run_ours(args, rank, world, local_rank):
             "roofline": {"bound": "hbm", "achieved": round(kernel_gbs, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(kernel_gbs / peak, 4), "peak_source": peak_kind,
                          "traffic": traffic,
-                         "kernel": "stripe_kernel<float,8,8,V=4,C=16> (gl_pbr_spmm: half-warps with float4 lanes, dynamic stripe draw)",
+                         "kernel": ("window_kernel<8> (gl_pbr_spmm kernel = 2: staged 64-row X windows)"
+                                    if args.kernel == "window" else
+                                    "stripe_kernel<float,8,8,V=4,C=16> (gl_pbr_spmm: half-warps with float4 "
+                                    "lanes, stripes drawn 64-row window by window)"),
                          "heavy_pieces": int(desc.num_pieces), "heavy_stripes": int(desc.num_heavy)},
             "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "ms_per_step": round(e2e_ms, 4),
                     "h2d_bytes_per_step": int(x_host.numel() * 4),
@@ -393,10 +399,10 @@ def run_ppr(dev, args) -> dict:
     references the GPU columns are compared with."""
     import torch
 
-    from page_rank_gb300 import synth
+    from page_rank_gb300 import synth, workloads
     from page_rank_gb300.autotune import autotune
     from page_rank_gb300.engine import PPREngine
-    from page_rank_gb300.warmstart import WarmStart, WarmStartGate
+    from page_rank_gb300.window_start import WindowStart
 
     K = 256
     t0 = time.perf_counter()
@@ -420,27 +426,27 @@ def run_ppr(dev, args) -> dict:
     eng.solve_plain(sets[:2], alpha=PPR_ALPHA, tol=PPR_TOL)
     rp = eng.solve_plain(sets[:plain_n], alpha=PPR_ALPHA, tol=PPR_TOL)
     sampler.stop()
-    # warm start: the network trained on plain-method vectors of this graph,
-    # used as configured (its gate predicts only when the estimated saving
-    # beats the prediction's cost; the first batch calibrates it) and forced
-    # on every column
-    ws = WarmStart(eng, seed=0, gate=WarmStartGate())
+    # warm start: the window-solve start (3 window exits, expected far
+    # field; its per-graph setup runs before the clock and is reported)
+    wst = WindowStart(eng, leaves=3)
     t0 = time.perf_counter()
-    stats = ws.train(num_vectors=args.ppr_train_vectors, batch=256, nodes_per_vector=512, epochs=3)
-    train_s = time.perf_counter() - t0
-    ws.solve(sets[:8], alpha=PPR_ALPHA, tol=PPR_TOL)         # warm-up and the gate's first measurement
+    wst.inverses(PPR_ALPHA)
     torch.cuda.synchronize(dev)
-    rw = ws.solve(sets, alpha=PPR_ALPHA, tol=PPR_TOL, retire=True, use_graphs=True)
-    gate = ws.gate.summary()
-    forced = WarmStart(eng, seed=0)
-    forced.mlp = ws.mlp
-    rf = forced.solve(sets, alpha=PPR_ALPHA, tol=PPR_TOL, retire=True, use_graphs=True)
+    warm_setup_s = time.perf_counter() - t0
+    wst.solve(sets[:8], alpha=PPR_ALPHA, tol=PPR_TOL)        # launch shapes and workspaces once
+    torch.cuda.synchronize(dev)
+    rw = wst.solve(sets, alpha=PPR_ALPHA, tol=PPR_TOL, retire=True, use_graphs=True)
     qps_b = K / rb.seconds
     qps_p = plain_n / rp.seconds
     qps_w = K / rw.seconds
-    qps_f = K / rf.seconds
-    same = float(max((rb.X.double() - rw.X.double()).abs().sum(dim=0).max().item(),
-                     (rb.X.double() - rf.X.double()).abs().sum(dim=0).max().item()))
+    same = float((rb.X.double() - rw.X.double()).abs().sum(dim=0).max().item())
+    # the warm-start configuration (2**21 nodes of the same class): cold and
+    # every start on the same held-out seed sets
+    layout = (tuned.block_size, tuned.min_nnz, tuned.column_tile)
+    del wst
+    torch.cuda.empty_cache()
+    wcfg = workloads.warmstart(dev, log2n=args.warm_log2n, train_vectors=args.ppr_train_vectors, K=K,
+                               layout=layout, mlp_start=False, keep_x=not args.no_cpu_baseline)
     out = {
         "workload": f"batched PPR: {g.description}; {K} seed sets of 1-32 uniform seeds, alpha {PPR_ALPHA}, "
                     f"per-column L1 {PPR_TOL:g} to the fixed point (certified stop), retirement + CUDA graphs",
@@ -451,27 +457,26 @@ def run_ppr(dev, args) -> dict:
                     "column_steps": rb.column_steps, "all_converged": bool(rb.converged.all())},
         "plain": {"queries_per_s": round(qps_p, 2), "sample": plain_n, "seconds": round(rp.seconds, 4),
                   "iterations_sum": int(rp.iterations.sum())},
-        "batched_warm": {"queries_per_s": round(qps_w, 2), "seconds_including_prediction": round(rw.seconds, 4),
+        "batched_warm": {"queries_per_s": round(qps_w, 2), "seconds_including_start": round(rw.seconds, 4),
+                         "start": "window-solve start: 3 window exits, expected far field, cold fallback",
+                         "setup_s": round(warm_setup_s, 2),
                          "iterations_sum": int(rw.iterations.sum()), "column_steps": rw.column_steps,
-                         "columns_using_prediction": float(np.mean(rw.warm_columns)),
-                         "gate": gate, "train_vectors": stats.vectors, "train_s": round(train_s, 2),
+                         "columns_using_start": float(np.mean(rw.warm_columns)),
                          "all_converged": bool(rw.converged.all())},
-        "batched_warm_forced": {"queries_per_s": round(qps_f, 2), "seconds_including_prediction": round(rf.seconds, 4),
-                                "iterations_sum": int(rf.iterations.sum()),
-                                "columns_using_prediction": float(np.mean(rf.warm_columns)),
-                                "all_converged": bool(rf.converged.all())},
         "speedup_batched_vs_plain": round(qps_b / qps_p, 2),
         "speedup_batched_warm_vs_plain": round(qps_w / qps_p, 2),
-        "iterations_cold_over_warm_forced": round(float(rb.iterations.sum()) / max(1, int(rf.iterations.sum())), 3),
+        "iterations_cold_over_warm": round(float(rb.iterations.sum()) / max(1, int(rw.iterations.sum())), 3),
+        "wall_cold_over_warm": round(rb.seconds / rw.seconds, 3),
         "max_l1_cold_vs_warm": same,
         "clocks": clocks,
+        "warm_start_config": {k: v for k, v in wcfg.items() if not k.startswith("_")},
     }
     if not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         sample = list(range(min(cores, K)))
         cpu = cpu_ppr_leg(g, [sets[i] for i in sample], cores)
         Xg = rb.X[:, torch.tensor(sample, device=dev)].double().cpu().numpy()
-        Xw = rf.X[:, torch.tensor(sample, device=dev)].double().cpu().numpy()
+        Xw = rw.X[:, torch.tensor(sample, device=dev)].double().cpu().numpy()
         d_b = np.abs(Xg - cpu["X"]).sum(axis=0) + cpu["bound"]
         d_w = np.abs(Xw - cpu["X"]).sum(axis=0) + cpu["bound"]
         out["parity"] = {"max_l1_vs_fp64": float(d_b.max()), "max_l1_warm_vs_fp64": float(d_w.max()),
@@ -484,7 +489,24 @@ def run_ppr(dev, args) -> dict:
                                          f"iteration (the reference update and stop rule, certified L1 "
                                          f"{PPR_TOL:g}), {cpu['seconds']:.1f} s wall"}
         out["speedup_batched_vs_cpu"] = round(qps_b / cpu["qps"], 1)
+        out["warm_start_config"]["parity"] = warm_config_parity(wcfg, cores)
     return out
+
+
+def warm_config_parity(wcfg: dict, cores: int, columns: int = 16) -> dict:
+    """The best warm start's columns of the warm-start configuration against
+    the FP64 fixed point: FP64 power iteration continued from them to a
+    certified distance (the CPU leg's checker)."""
+    from oracle.ppr import refine_fp64, teleport_matrix
+
+    g = wcfg["_graph"]
+    sets = wcfg["_sets"][:columns]
+    X = wcfg["_X_best"][:, :columns].double().cpu().numpy()
+    V = teleport_matrix(g.n, sets)
+    ref, cert, its = refine_fp64(g.A, X, V, PPR_ALPHA, g.dangling, 1e-9, threads=cores)
+    d = np.abs(X - ref).sum(axis=0) + cert
+    return {"start": wcfg["best"], "columns": len(sets), "max_l1_vs_fp64": float(d.max()), "tol": PPR_TOL,
+            "reference": f"FP64 power iteration from the GPU columns to a certified distance < {cert.max():.1e}"}
 
 
 def _ppr_worker(args):
@@ -662,19 +684,24 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ppr", action="store_true", help="skip the PPR queries/s part of the line")
+    ap.add_argument("--kernel", choices=["auto", "stripe", "window"], default="auto",
+                    help="SpMM kernel (auto: the library's choice, the stripe kernel)")
     ap.add_argument("--ppr-log2n", type=int, default=22)
-    ap.add_argument("--ppr-train-vectors", type=int, default=2048)
+    ap.add_argument("--ppr-train-vectors", type=int, default=1024)
+    ap.add_argument("--warm-log2n", type=int, default=21)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
-    ap.add_argument("--log2n", type=int, default=20,
-                    help="graph size (2**log2n nodes); only for small profiling runs")
-    ap.add_argument("--workload", choices=["spmm", "ppr_small", "ppr_batched", "warmstart", "serving", "kernels",
-                                           "edges"],
+    ap.add_argument("--log2n", type=int, default=None,
+                    help="graph size (2**log2n nodes); default: the workload's configuration size")
+    ap.add_argument("--workload", choices=["spmm", "ppr_small", "ppr_batched", "ppr_step", "warmstart", "serving",
+                                           "kernels", "edges"],
                     default="spmm",
                     help="spmm (default, the headline line) or a secondary PPR workload")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
 
+    if args.workload == "spmm" and args.log2n is None:
+        args.log2n = 20
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
@@ -685,9 +712,9 @@ def main():
         dev = torch.device("cuda", local_rank)
         torch.cuda.set_device(dev)
         fn = getattr(workloads, args.workload)
-        default_log2n = {"ppr_batched": 22, "warmstart": 21, "kernels": 20, "edges": 20}
+        default_log2n = {"ppr_batched": 22, "ppr_step": 22, "warmstart": 21, "kernels": 20, "edges": 20}
         out = fn(dev) if args.workload in ("ppr_small", "serving") else \
-            fn(dev, log2n=args.log2n if args.log2n != 20 else default_log2n[args.workload])
+            fn(dev, log2n=args.log2n if args.log2n is not None else default_log2n[args.workload])
         out = {"workload": args.workload, **out}
     elif args.impl == "reference":
         out = run_reference(args, rank, world)

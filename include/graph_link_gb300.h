@@ -441,6 +441,52 @@ int gl_mlp_adam(float* params, const float* grad, float* m, float* v, int64_t co
                 float beta1, float beta2, float eps, float grad_scale, int32_t step,
                 uint16_t* W1_bf16, uint16_t* w2_bf16, int32_t f_in, cudaStream_t stream);
 
+/* ======================================================================== */
+/* Window-solve warm start                                                  */
+/* No counterpart in the reference (its iterate starts from the seed        */
+/* indicators, Backend/graph_link/kernels/ppr_kernel.cu:199-209).  The node */
+/* order is cut into windows of 64 rows; B = I - alpha blockdiag(A_w) over  */
+/* the 64 x 64 diagonal window blocks A_w of the transition matrix, stored  */
+/* as ceil(n / 64) dense row-major FP32 blocks (rows past n are identity).  */
+/* ======================================================================== */
+
+/* blocks[w] = I - alpha A_w from the device CSR of A (int32 indptr /
+ * indices, FP32 data; entries of a row whose column is outside the row's
+ * window are skipped).  alpha in [0, 1). */
+int gl_window_blocks(const int32_t* indptr, const int32_t* indices, const float* data, int64_t n, float alpha,
+                     float* blocks, cudaStream_t stream);
+
+/* Inverts every block in place (Gauss-Jordan without pivoting, valid for
+ * strictly column diagonally dominant blocks: columns of A summing to at
+ * most 1).  *status (device int32) is set to 0, then to 1 if a pivot was
+ * not positive and finite; the caller reads it after the stream. */
+int gl_window_invert(float* blocks, int64_t n, int32_t* status, cudaStream_t stream);
+
+/* Y = scale * B^-1 T window by window (T, Y, near_field: [n][K] row-major
+ * FP32); near_field = near_scale * Y (near_init = 1) or += (near_init = 0),
+ * and partial[w][K] = (or +=) the column sums of near_scale * Y over window w
+ * (partial may be NULL).  Y or near_field may be NULL, not both. */
+int gl_window_apply(const float* inverses, int64_t n, int32_t K, const float* T, float scale, float* Y,
+                    float* near_field, float near_scale, int32_t near_init, float* partial, cudaStream_t stream);
+
+/* Device workspace (bytes) for gl_window_finalize; -1 for negative sizes. */
+int64_t gl_window_finalize_workspace_bytes(int64_t n, int32_t K);
+
+/* near_field[i][c] += max(0, 1 - sum_w partial[w][c]) * shape[i]: the mass a
+ * truncated near field misses, placed along shape (FP32 [n], summing to 1). */
+int gl_window_finalize(float* near_field, int64_t n, int32_t K, const float* partial, const float* shape,
+                       void* workspace, int64_t workspace_bytes, cudaStream_t stream);
+
+/* Residual of one PPR step from the teleport vector, per column:
+ * out[c] = || P(v_c) - v_c ||_1 for P(x) = alpha A x + ((1 - alpha) +
+ * alpha d(x)) v_c, d(x) the mass on dangling nodes (bitmap, may be NULL).
+ * colsum[j] = sum_i A[i][j] (FP64).  The seed sets are the teleport index
+ * (seed_ptr [K + 1], unique seed_rows, seed_weights); A's column indices
+ * must be sorted within each row.  A seed outside [0, n) gives -1. */
+int gl_cold_residual(const int32_t* indptr, const int32_t* indices, const float* data, const double* colsum,
+                     const uint32_t* dangling_bits, int64_t n, const int32_t* seed_ptr, const int32_t* seed_rows,
+                     const float* seed_weights, int32_t K, float alpha, double* out, cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

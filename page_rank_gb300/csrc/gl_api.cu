@@ -267,7 +267,7 @@ __global__ void counter_add_kernel(int32_t* c, int32_t d) { *c += d; }
 using namespace gl;
 
 extern "C" const char* gl_last_error(void) { return last_error(); }
-extern "C" int gl_version(void) { return 101; }
+extern "C" int gl_version(void) { return 102; }
 
 extern "C" int64_t gl_pbr_spmm_workspace_bytes(const gl_pbr_matrix* A, int64_t batch, int64_t features) {
     if (A == nullptr || batch < 0 || features < 0) return -1;

@@ -73,6 +73,8 @@ class PPREngine:
             data = torch.from_numpy(A.data.astype(np.float32)).to(self.device)
             self.pbr = pbr_from_device_csr(indptr, indices, data, self.n, self.n, self.block_size,
                                            self.block_size, self.min_nnz)
+            # the device CSR stays resident for the window-solve warm start
+            self.csr = (indptr, indices, data)
             self.mat = self.pbr.to(self.device)
             from .graph_link.pbr_registry import get_pbr_gpu_meta
             self.meta = get_pbr_gpu_meta(self.mat)
@@ -129,9 +131,10 @@ class PPREngine:
         return (torch.from_numpy(ptr2).to(dev), torch.from_numpy(rows).to(dev),
                 torch.from_numpy(w).to(dev))
 
-    def teleport_columns(self, seed_sets) -> torch.Tensor:
-        """Dense teleport (personalization) vectors [n, K] of the seed sets."""
-        ptr, rows, w = self.teleport(seed_sets)
+    def teleport_columns(self, seed_sets, tel: tuple | None = None) -> torch.Tensor:
+        """Dense teleport (personalization) vectors [n, K] of the seed sets
+        (``tel``: their ``teleport()`` index, when the caller has it)."""
+        ptr, rows, w = self.teleport(seed_sets) if tel is None else tel
         tp = teleport_from_seed_sets(ptr, rows, self.n, self.block_size, w)
         V = torch.empty((self.n, len(seed_sets)), dtype=torch.float32, device=self.device)
         native.check(native.lib().gl_ppr_init(tp.desc(), self.n, len(seed_sets), native.GL_F32, V.data_ptr(),
@@ -159,8 +162,12 @@ class PPREngine:
         dev = self.device
         t0 = time.perf_counter()   # the solve's time includes the warm start's prediction
         warm_columns = None
+        pre_steps = 0
         if warm_start is not None and x0 is None:
             x0, warm_columns = warm_start.start_vectors(seed_sets, alpha)
+            # steps the start already took from its vector (they count as
+            # iterations of the columns that kept it)
+            pre_steps = int(getattr(warm_start, "pre_steps", 0))
         thr = certified_tolerance(tol, alpha) if certified else tol
         with torch.cuda.device(dev):
             ptr, rows, w = self.teleport(seed_sets)
@@ -227,6 +234,12 @@ class PPREngine:
                 else:
                     active = active[:0]
             torch.cuda.synchronize(dev)
+        if isinstance(warm_columns, torch.Tensor):
+            warm_columns = warm_columns.cpu().numpy()
+        if pre_steps:
+            col_iter[np.asarray(warm_columns, bool) & (col_iter >= 0)] += pre_steps
+            launched += pre_steps
+            column_steps += pre_steps * K
         res = BatchResult(X=out, iterations=col_iter, launched_iterations=launched,
                           converged=col_iter >= 0, seconds=time.perf_counter() - t0,
                           column_steps=column_steps, history=history)

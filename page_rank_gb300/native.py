@@ -186,6 +186,12 @@ _SIGS = {
     "gl_mlp_backward": (_c.c_int, [_vp, _vp, _i64, _i32, _vp, _vp, _vp, _c.c_float, _vp, _vp, _vp]),
     "gl_mlp_adam": (_c.c_int, [_vp, _vp, _vp, _vp, _i64, _c.c_float, _c.c_float, _c.c_float, _c.c_float,
                                _c.c_float, _i32, _vp, _vp, _i32, _vp]),
+    "gl_window_blocks": (_c.c_int, [_vp, _vp, _vp, _i64, _c.c_float, _vp, _vp]),
+    "gl_window_invert": (_c.c_int, [_vp, _i64, _vp, _vp]),
+    "gl_window_apply": (_c.c_int, [_vp, _i64, _i32, _vp, _c.c_float, _vp, _vp, _c.c_float, _i32, _vp, _vp]),
+    "gl_window_finalize_workspace_bytes": (_i64, [_i64, _i32]),
+    "gl_window_finalize": (_c.c_int, [_vp, _i64, _i32, _vp, _vp, _vp, _i64, _vp]),
+    "gl_cold_residual": (_c.c_int, [_vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _i32, _c.c_float, _vp, _vp]),
 }
 
 

@@ -75,6 +75,7 @@ class _Group:
         self.reqs: list[Request] = []          # live columns, in column order
         self.col_iters: list[int] = []         # iterations run per live column
         self.joining: list[Request] = []
+        self.pre_pending = None                 # (first column, iterations already taken) of joiners
         self.run: PprRun | None = None
         self.x = None                          # current iterate [n, K]
         self.pending = False                   # a chunk is in flight on self.stream
@@ -101,12 +102,17 @@ class _Group:
                 if x_keep is not None and self.reqs:
                     x0[:, : len(self.reqs)] = x_keep
                 j0 = len(self.reqs)
-                x_new = self.server.start_vectors(self.graph, [r.seeds for r in self.joining],
-                                                  np.array([r.alpha for r in self.joining]), self.stream)
+                x_new, pre = self.server.start_vectors(self.graph, [r.seeds for r in self.joining],
+                                                       np.array([r.alpha for r in self.joining]), self.stream)
                 x0[:, j0:] = x_new
             else:
                 x0 = x_keep
+                pre = None
             run.init(x0)
+        if pre is not None:
+            # iterations the start already took, per joining column: a device
+            # tensor, read at the next harvest (which waits for the stream)
+            self.pre_pending = (len(self.col_iters), pre)
         self.col_iters = self.col_iters + [0] * len(self.joining)
         self.reqs = reqs
         self.joining = []
@@ -127,6 +133,12 @@ class _Group:
         with torch.cuda.stream(self.stream):
             res = run.res_hist[t0:t0 + n_valid].cpu().numpy() if n_valid > 0 else \
                 np.zeros((0, len(self.reqs)))
+            if self.pre_pending is not None:
+                j0, pre = self.pre_pending
+                pre = pre.cpu().numpy() if isinstance(pre, torch.Tensor) else np.asarray(pre)
+                for i, p in enumerate(pre):
+                    self.col_iters[j0 + i] += int(p)
+                self.pre_pending = None
         self.chunk_steps += chunk
         self.pending = False
         finished = []
@@ -227,15 +239,28 @@ class PPRServer:
             tot += (len(g.reqs) + len(g.joining)) * self.column_bytes(g.graph)
         return tot
 
-    def start_vectors(self, graph: str, seed_sets, alpha, stream) -> torch.Tensor:
-        """Initial columns for newly admitted requests: learned warm start where
-        available (with its cold-start fallback), else the teleport vector."""
+    def start_vectors(self, graph: str, seed_sets, alpha, stream):
+        """(initial columns, iterations already taken per column) for newly
+        admitted requests: the graph's warm start where it has one (with its
+        cold-start fallback; requests are grouped by damping factor, which
+        the start's precomputation depends on), else the teleport vectors."""
         eng = self.engines[graph]
         ws = self.warm.get(graph)
+        k = len(seed_sets)
         with torch.cuda.stream(stream):
             if ws is None:
-                return eng.teleport_columns(seed_sets)
-            return ws.start_vectors(seed_sets, alpha)[0]
+                return eng.teleport_columns(seed_sets), np.zeros(k, dtype=np.int64)
+            alpha = np.broadcast_to(np.asarray(alpha, dtype=np.float64), (k,))
+            X = torch.empty((eng.n, k), dtype=torch.float32, device=eng.device)
+            pre = torch.zeros(k, dtype=torch.int64, device=eng.device)     # read at the next harvest
+            for a in np.unique(alpha):
+                sel = np.nonzero(alpha == a)[0]
+                idx = torch.from_numpy(sel).pin_memory().to(eng.device, non_blocking=True)
+                xs, used = ws.start_vectors([seed_sets[i] for i in sel], float(a))
+                X[:, idx] = xs
+                used = torch.as_tensor(used, device=eng.device)
+                pre[idx] = used.to(torch.int64) * int(getattr(ws, "pre_steps", 0))
+            return X, pre
 
     # -- requests -----------------------------------------------------------------
     def submit(self, graph: str, seeds, alpha: float = 0.85, tol: float = 1e-6,

@@ -49,21 +49,25 @@ LOG_FLOOR = 1e-10
 class MLP:
     """Parameters and optimizer state of the warm-start network (device)."""
 
-    def __init__(self, device, seed: int = 0):
+    def __init__(self, device, seed: int = 0, f_in: int = F_IN, out_bias: float = math.log(1e-7)):
+        if not 1 <= f_in <= native.GL_MLP_MAX_IN:
+            raise ValueError(f"f_in must be in 1..{native.GL_MLP_MAX_IN}")
+        self.f_in = f_in = int(f_in)
+        n_params = HIDDEN * f_in + 2 * HIDDEN + 1
         g = torch.Generator().manual_seed(seed)
-        p = torch.zeros(N_PARAMS, dtype=torch.float32)
-        bound1 = 1.0 / math.sqrt(F_IN)
-        p[: HIDDEN * F_IN] = (torch.rand(HIDDEN * F_IN, generator=g) * 2 - 1) * bound1
-        p[HIDDEN * F_IN: HIDDEN * F_IN + HIDDEN] = 0.01
+        p = torch.zeros(n_params, dtype=torch.float32)
+        bound1 = 1.0 / math.sqrt(f_in)
+        p[: HIDDEN * f_in] = (torch.rand(HIDDEN * f_in, generator=g) * 2 - 1) * bound1
+        p[HIDDEN * f_in: HIDDEN * f_in + HIDDEN] = 0.01
         bound2 = 1.0 / math.sqrt(HIDDEN)
-        p[HIDDEN * F_IN + HIDDEN: HIDDEN * F_IN + 2 * HIDDEN] = (torch.rand(HIDDEN, generator=g) * 2 - 1) * bound2
-        p[-1] = math.log(1e-7)
+        p[HIDDEN * f_in + HIDDEN: HIDDEN * f_in + 2 * HIDDEN] = (torch.rand(HIDDEN, generator=g) * 2 - 1) * bound2
+        p[-1] = out_bias
         self.device = device
         self.params = p.to(device)
         self.m = torch.zeros_like(self.params)
         self.v = torch.zeros_like(self.params)
         self.grad = torch.zeros_like(self.params)
-        self.W1 = torch.zeros(HIDDEN * F_IN, dtype=torch.int16, device=device)
+        self.W1 = torch.zeros(HIDDEN * f_in, dtype=torch.int16, device=device)
         self.w2 = torch.zeros(HIDDEN, dtype=torch.int16, device=device)
         self.loss = torch.zeros(1, dtype=torch.float64, device=device)
         self.step = 0
@@ -76,12 +80,13 @@ class MLP:
             lsb = (u >> 16) & 1
             r = (u + 0x7FFF + lsb) >> 16
             return (r & 0xFFFF).to(torch.int32).to(torch.int16)
-        self.W1.copy_(to_bf16_bits(self.params[: HIDDEN * F_IN]))
-        self.w2.copy_(to_bf16_bits(self.params[HIDDEN * F_IN + HIDDEN: HIDDEN * F_IN + 2 * HIDDEN]))
+        f = self.f_in
+        self.W1.copy_(to_bf16_bits(self.params[: HIDDEN * f]))
+        self.w2.copy_(to_bf16_bits(self.params[HIDDEN * f + HIDDEN: HIDDEN * f + 2 * HIDDEN]))
 
     @property
     def b1(self) -> torch.Tensor:
-        return self.params[HIDDEN * F_IN: HIDDEN * F_IN + HIDDEN]
+        return self.params[HIDDEN * self.f_in: HIDDEN * self.f_in + HIDDEN]
 
     def b2(self) -> float:
         return float(self.params[-1].item())
@@ -90,7 +95,7 @@ class MLP:
         X = X.contiguous()
         out = torch.empty(X.shape[0], dtype=torch.float32, device=self.device)
         native.check(native.lib().gl_mlp_forward(
-            _ptr(X), X.shape[0], F_IN, self.W1.data_ptr(), self.b1.data_ptr(), self.w2.data_ptr(),
+            _ptr(X), X.shape[0], self.f_in, self.W1.data_ptr(), self.b1.data_ptr(), self.w2.data_ptr(),
             self.b2() if b2 is None else b2, _ptr(out), torch.cuda.current_stream(self.device).cuda_stream))
         return out
 
@@ -98,7 +103,7 @@ class MLP:
         self.grad.zero_()
         self.loss.zero_()
         native.check(native.lib().gl_mlp_backward(
-            _ptr(X.contiguous()), _ptr(target.contiguous()), X.shape[0], F_IN, self.W1.data_ptr(),
+            _ptr(X.contiguous()), _ptr(target.contiguous()), X.shape[0], self.f_in, self.W1.data_ptr(),
             self.b1.data_ptr(), self.w2.data_ptr(), self.b2(), self.grad.data_ptr(), self.loss.data_ptr(),
             torch.cuda.current_stream(self.device).cuda_stream))
         return self.grad, float(self.loss.item())
@@ -106,9 +111,9 @@ class MLP:
     def adam_step(self, n_examples: int, lr: float = 2e-3):
         self.step += 1
         native.check(native.lib().gl_mlp_adam(
-            self.params.data_ptr(), self.grad.data_ptr(), self.m.data_ptr(), self.v.data_ptr(), N_PARAMS,
-            lr, 0.9, 0.999, 1e-8, 1.0 / max(1, n_examples), self.step, self.W1.data_ptr(),
-            self.w2.data_ptr(), F_IN, torch.cuda.current_stream(self.device).cuda_stream))
+            self.params.data_ptr(), self.grad.data_ptr(), self.m.data_ptr(), self.v.data_ptr(),
+            self.params.numel(), lr, 0.9, 0.999, 1e-8, 1.0 / max(1, n_examples), self.step, self.W1.data_ptr(),
+            self.w2.data_ptr(), self.f_in, torch.cuda.current_stream(self.device).cuda_stream))
 
 
 @dataclass
@@ -337,3 +342,105 @@ class WarmStart:
         e1.record()
         res = run.res_hist[0].cpu().numpy()
         return res, e0.elapsed_time(e1) / 2e3
+
+
+FAR_F_IN = 6
+
+
+class FarFieldModel:
+    """Learned far-field shape for the window-solve start
+    (``window_start.WindowStart(shape="learned")``).
+
+    The window start computes a query's near field exactly and must place
+    the mass it misses (the walks that leave their window more often than the
+    start follows them) somewhere.  This network predicts, per node, the log
+    density of that far field from a per-graph basis of vectors computed
+    once (PageRank, the near field of the uniform teleport vector and that
+    vector's far field) and node features:
+
+      log(n PageRank_i), log(n near_i), log(n far_i), log(1 + in-degree),
+      log(1 + out-degree), and the transition mass that leaves i's window.
+
+    It is trained on far fields of PPR vectors the plain method computed
+    (the batched engine without a warm start): for each training column the
+    exact vector minus the window start's near field, normalized, averaged
+    over the columns, with nodes sampled by mass (most) and uniformly.  For
+    seed sets drawn uniformly at random that average tends to the uniform
+    vector's far field (PPR is linear in the teleport vector), so the basis
+    vector ``far`` is already close to the target; the network learns the
+    per-node correction between the two."""
+
+    def __init__(self, device, seed: int = 0):
+        self.device = device
+        self.mlp = MLP(device, seed, f_in=FAR_F_IN, out_bias=0.0)
+        self.stats: TrainStats | None = None
+        self._shapes: dict = {}
+
+    def features(self, ws, alpha: float) -> torch.Tensor:
+        st = ws._prepare(alpha)
+        eng = ws.eng
+        n = eng.n
+        dev = self.device
+        indptr, indices, _ = eng.csr
+        in_deg = (indptr[1:] - indptr[:-1]).to(torch.float32)
+        out_deg = torch.bincount(indices.to(torch.int64), minlength=n).to(torch.float32)
+        f = torch.empty((n, FAR_F_IN), dtype=torch.float32, device=dev)
+        f[:, 0] = torch.log(n * st["pagerank"].clamp_min(0) + 1e-6) / 10.0
+        f[:, 1] = torch.log(n * st["near_uniform"].clamp_min(0) + 1e-6) / 10.0
+        f[:, 2] = torch.log(n * st["expected"].clamp_min(0) + 1e-6) / 10.0
+        f[:, 3] = torch.log1p(in_deg)
+        f[:, 4] = torch.log1p(out_deg)
+        f[:, 5] = ws.off.leak
+        return f
+
+    def fit(self, ws, alpha: float, seed_sets, tol: float = 1e-6, epochs: int = 30, minibatch: int = 8192,
+            lr: float = 3e-3, samples_per_epoch: int = 1 << 20, seed: int = 100, batch: int = 256) -> TrainStats:
+        """Train on the far fields of ``seed_sets`` solved by the plain method
+        (in slices of ``batch`` columns)."""
+        t0 = time.perf_counter()
+        eng = ws.eng
+        n = eng.n
+        acc = torch.zeros(n, dtype=torch.float64, device=self.device)
+        for c0 in range(0, len(seed_sets), batch):
+            sl = seed_sets[c0:c0 + batch]
+            res = eng.solve(sl, alpha=alpha, tol=tol)
+            V = eng.teleport_columns(sl)
+            near, _ = ws._near_field(V, alpha, keep_v=False)
+            far = (res.X - near).clamp_min(0)
+            far = far / far.sum(dim=0, keepdim=True).clamp_min(1e-30)
+            acc += far.sum(dim=1, dtype=torch.float64)
+            del far, near, V, res
+        target_mass = (acc / max(1, len(seed_sets))).to(torch.float32)   # [n], sums to 1
+        T = torch.log(n * target_mass + 1e-6)
+        F = self.features(ws, alpha)
+        gen = torch.Generator(device=self.device).manual_seed(seed)
+        losses = []
+        steps_total = epochs * ((samples_per_epoch + minibatch - 1) // minibatch)
+        step = 0
+        for _ in range(epochs):
+            n_mass = samples_per_epoch * 3 // 4
+            idx = torch.cat([torch.multinomial(target_mass + 1e-12, n_mass, replacement=True, generator=gen),
+                             torch.randint(0, n, (samples_per_epoch - n_mass,), device=self.device,
+                                           generator=gen)])
+            idx = idx[torch.randperm(idx.numel(), device=self.device, generator=gen)]
+            for s0 in range(0, idx.numel(), minibatch):
+                sel = idx[s0:s0 + minibatch]
+                _, loss = self.mlp.gradient(F[sel], T[sel])
+                cur = lr * (0.1 + 0.9 * 0.5 * (1.0 + math.cos(math.pi * step / max(1, steps_total))))
+                self.mlp.adam_step(sel.numel(), cur)
+                losses.append(loss / sel.numel())
+                step += 1
+        torch.cuda.synchronize(self.device)
+        self._shapes.clear()
+        self.stats = TrainStats(vectors=len(seed_sets), examples=epochs * samples_per_epoch,
+                                seconds=time.perf_counter() - t0, losses=losses)
+        return self.stats
+
+    def shape(self, ws, alpha: float) -> torch.Tensor:
+        """Predicted far-field density [n] (sums to 1) for this graph and alpha."""
+        key = (id(ws), round(float(alpha), 12))
+        if key not in self._shapes:
+            y = self.mlp.forward(self.features(ws, alpha))
+            x = torch.exp(y - y.max())
+            self._shapes[key] = (x / x.sum()).contiguous()
+        return self._shapes[key]

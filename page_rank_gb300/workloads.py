@@ -82,50 +82,211 @@ def ppr_batched(device, log2n: int = 22, K: int = 256, plain_sample: int = 16, t
     }
 
 
-def warmstart(device, log2n: int = 21, train_vectors: int = 20000, K: int = 256) -> dict:
-    """Learned warm start on the cluster / Zipf graph class at n = 2**log2n:
-    train on ``train_vectors`` plain-method PPR vectors (seed sets of 1-32),
-    then solve K held-out seed sets from the predicted start and from the
-    cold start, both to the certified L1 1e-6."""
-    from .warmstart import WarmStart
+def ppr_step(device, log2n: int = 22, K: int = 256, block: int = 4, min_nnz: int = 4, tile: int = 0,
+             steps: int = 16) -> dict:
+    """Fused power-iteration steps alone (``gl_ppr_step``, STOP_ALL, dense
+    start columns) on the batched configuration's graph class with K
+    columns: the kernel behind the batched queries/s, timed with CUDA events
+    over ``steps`` steps after four warm-up steps."""
+    from .graph_link.pbr_registry import get_pbr_gpu_meta
+    from .pbr import pbr_from_device_csr
+    from .ppr import PprRun, dangling_bitmap, teleport_from_seed_sets
     g = synth.cluster_zipf_graph(log2n=log2n, mean_degree=20.0, seed=3, device=device)
-    eng = PPREngine(g.A, block_size=8, min_nnz_per_block=4, device=device, dangling=g.dangling)
-    ws = WarmStart(eng, seed=0)
-    stats = ws.train(num_vectors=train_vectors, batch=256, nodes_per_vector=512, epochs=3)
-    sets = synth.seed_sets(g.n, K, 1, 32, seed=424242)
-    eng.solve(sets[:8], tol=1e-6)
+    A = g.A
+    n = A.shape[0]
+    indptr = torch.from_numpy(A.indptr.astype(np.int32)).to(device)
+    indices = torch.from_numpy(A.indices.astype(np.int32)).to(device)
+    data = torch.from_numpy(A.data.astype(np.float32)).to(device)
+    dbits = dangling_bitmap(indices, n)
+    pbr = pbr_from_device_csr(indptr, indices, data, n, n, block, block, min_nnz).to(device)
+    meta = get_pbr_gpu_meta(pbr)
+    meta["column_tile"] = tile
+    rng = np.random.default_rng(0)
+    seeds = torch.from_numpy(rng.integers(0, n, K).astype(np.int32)).to(device)
+    sptr = torch.arange(K + 1, dtype=torch.int32, device=device)
+    x = torch.rand((n, K), generator=torch.Generator(device=device).manual_seed(0), device=device)
+    x /= x.sum(dim=0, keepdim=True)
+    tp = teleport_from_seed_sets(sptr, seeds, n, block)
+    run = PprRun(meta, n, n, block, block, tp, 0.85, steps + 4, 0.0, native.GL_PPR_STOP_ALL, dbits)
+    run.init(x)
+    run.launch_chunk(4)
     torch.cuda.synchronize(device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    run.launch_chunk(steps)
+    e1.record()
+    torch.cuda.synchronize(device)
+    ms = e0.elapsed_time(e1) / steps
+    nb, packed, rem = meta["codes"].numel(), meta["data"].numel(), meta["rem_col_ind"].numel()
+    B = 20 * nb + 4 * packed + 4 * (n + 1) + 8 * rem + 8 * n * K
+    return {"workload": f"ppr_step: {g.description}, K={K} dense columns, PBR {block}x{block} min {min_nnz}, "
+                        f"column tile {tile or 'automatic'}",
+            "n": n, "nnz": int(A.nnz), "ms_per_step": round(ms, 4), "alg_bytes_per_step": B,
+            "alg_GBs": round(B / ms / 1e6, 1)}
+
+
+def warmstart(device, log2n: int = 21, train_vectors: int = 20000, K: int = 256, leaves=(2, 3, 4, 6, 8),
+              layout=(4, 4, 0), mlp_start: bool = True, keep_x: bool = False) -> dict:
+    """Warm starts on the cluster / Zipf graph class at n = 2**log2n, K held-out
+    seed sets of 1-32 seeds, alpha 0.85, certified L1 1e-6, each solved cold
+    and from every start (wall time includes computing the start):
+
+    * the window-solve start with the global PageRank vector as far field,
+      with the far field learned by ``FarFieldModel`` (trained on
+      ``train_vectors`` plain-method vectors), and with the expected far
+      field, for each number of window exits in ``leaves``;
+    * with ``mlp_start``, the per-(node, query) network start
+      (``WarmStart``, trained on the same number of vectors).
+
+    The window start's per-graph setup (inverses, PageRank, far field) and the
+    networks' training run before the timed solves and are reported."""
+    from .warmstart import FarFieldModel, WarmStart
+    from .window_start import WindowStart
+    alpha, tol = 0.85, 1e-6
+    g = synth.cluster_zipf_graph(log2n=log2n, mean_degree=20.0, seed=3, device=device)
+    bs, mn, ct = layout
+    eng = PPREngine(g.A, block_size=bs, min_nnz_per_block=mn, device=device, dangling=g.dangling, column_tile=ct)
+    sets = synth.seed_sets(g.n, K, 1, 32, seed=424242)
+    eng.solve(sets[:8], alpha=alpha, tol=tol)
+    torch.cuda.synchronize(device)
+
+    def timed(fn):
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize(device)
+        return r, time.perf_counter() - t0
+
+    cold, t_cold = timed(lambda: eng.solve(sets, alpha=alpha, tol=tol))
+
+    def record(res, secs):
+        return {"iterations_sum": int(res.iterations.sum()), "iterations_mean": round(float(res.iterations.mean()), 2),
+                "iterations_max": int(res.iterations.max()), "seconds": round(secs, 4),
+                "queries_per_s": round(K / secs, 1), "column_steps": res.column_steps,
+                "columns_using_start": float(np.mean(getattr(res, "warm_columns", np.zeros(1)))),
+                "all_converged": bool(res.converged.all()),
+                "iterations_cold_over_this": round(float(cold.iterations.sum()) / max(1, int(res.iterations.sum())), 3),
+                "wall_cold_over_this": round(t_cold / secs, 3),
+                "max_l1_vs_cold": float((res.X.double() - cold.X.double()).abs().sum(dim=0).max().item())}
+
+    out = {"workload": f"warm starts: {g.description}; {K} held-out seed sets of 1-32 uniform seeds, alpha {alpha}, "
+                       f"certified L1 {tol:g}, PBR {bs}x{bs} min {mn}",
+           "n": g.n, "nnz": int(g.A.nnz), "cold": record(cold, t_cold), "starts": {}}
+    ws = WindowStart(eng, leaves=max(leaves), shape="pagerank")
+    _, setup = timed(lambda: ws.inverses(alpha))
+    out["window_setup_s"] = round(setup, 3)
+    out["off_window_nnz"] = ws.off.nnz
+    best = None
+    for L in leaves:
+        ws.leaves = L
+        ws.set_shape("expected")
+        ws.solve(sets[:8], alpha=alpha, tol=tol)
+        res, t = timed(lambda: ws.solve(sets, alpha=alpha, tol=tol))
+        _, t_start = timed(lambda: ws.start(sets, alpha))
+        rec = record(res, t)
+        rec["start_seconds"] = round(t_start, 4)
+        out["starts"][f"window_expected_L{L}"] = rec
+        if best is None or t < best[1]:
+            best = (f"window_expected_L{L}", t, res, L)
+    L = best[3]
+    ws.leaves = L
+    ws.set_shape("pagerank")
+    res, t = timed(lambda: ws.solve(sets, alpha=alpha, tol=tol))
+    out["starts"][f"window_pagerank_L{L}"] = record(res, t)
+    model = FarFieldModel(device, seed=0)
+    train_sets = synth.seed_sets(g.n, train_vectors, 1, 32, seed=7)
     t0 = time.perf_counter()
-    cold = eng.solve(sets, tol=1e-6)
-    t_cold = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    warm = ws.solve(sets, tol=1e-6)
-    t_warm = time.perf_counter() - t0
-    diff = (cold.X.double() - warm.X.double()).abs().sum(dim=0).max().item()
-    return {
-        "workload": f"warmstart: {g.description}, MLP 10-128-1 BF16 weights, trained on {train_vectors} "
-                    f"plain-method vectors, {K} held-out seed sets of 1-32",
-        "n": g.n, "nnz": int(g.A.nnz),
-        "train": {"vectors": stats.vectors, "examples": stats.examples, "seconds": round(stats.seconds, 2),
-                  "loss_first": stats.losses[0], "loss_last": stats.losses[-1]},
-        "cold": {"iterations_sum": int(cold.iterations.sum()), "iterations_max": int(cold.iterations.max()),
-                 "seconds": round(t_cold, 4), "column_steps": cold.column_steps},
-        "warm": {"iterations_sum": int(warm.iterations.sum()), "iterations_max": int(warm.iterations.max()),
-                 "seconds_including_prediction": round(t_warm, 4), "column_steps": warm.column_steps,
-                 "columns_using_prediction": float(warm.warm_columns.mean())},
-        "iteration_ratio_cold_over_warm": round(float(cold.iterations.sum() / max(1, warm.iterations.sum())), 3),
-        "max_l1_cold_vs_warm": diff,
-    }
+    stats = model.fit(ws, alpha, train_sets, tol=tol)
+    train_s = time.perf_counter() - t0
+    ws.set_shape("learned", model)
+    res, t = timed(lambda: ws.solve(sets, alpha=alpha, tol=tol))
+    rec = record(res, t)
+    rec["train"] = {"vectors": stats.vectors, "examples": stats.examples, "seconds": round(train_s, 2),
+                    "loss_first": round(stats.losses[0], 4), "loss_last": round(stats.losses[-1], 4)}
+    pr = out["starts"][f"window_pagerank_L{L}"]["iterations_sum"]
+    rec["iterations_pagerank_far_field_over_this"] = round(pr / max(1, int(res.iterations.sum())), 3)
+    out["starts"][f"window_learned_L{L}"] = rec
+    ws.set_shape("expected")
+    if mlp_start:
+        mw = WarmStart(eng, seed=0)
+        t0 = time.perf_counter()
+        ms = mw.train(num_vectors=train_vectors, batch=256, nodes_per_vector=512, epochs=3)
+        mt = time.perf_counter() - t0
+        res, t = timed(lambda: mw.solve(sets, alpha=alpha, tol=tol))
+        rec = record(res, t)
+        rec["train"] = {"vectors": ms.vectors, "examples": ms.examples, "seconds": round(mt, 2)}
+        out["starts"]["mlp_node_query"] = rec
+    out["start_kernels"] = window_start_kernels(ws, K)
+    out["best"] = best[0]
+    out["best_iterations_cold_over_warm"] = out["starts"][best[0]]["iterations_cold_over_this"]
+    out["best_wall_cold_over_warm"] = out["starts"][best[0]]["wall_cold_over_this"]
+    if keep_x:
+        out["_X_best"] = best[2].X
+        out["_sets"] = sets
+        out["_graph"] = g
+    return out
+
+
+def window_start_kernels(ws, K: int, reps: int = 5) -> dict:
+    """CUDA-event times of the window start's two kernels on K columns:
+    ``gl_window_apply`` (accumulating, with Y) and the off-window SpMM.
+    Algorithmic bytes of one apply: the inverses (16 KB per window), T read,
+    Y written, the near field read and written, the per-window sums read
+    and written; FLOPs 2 * 64 per output entry."""
+    eng = ws.eng
+    dev = ws.dev
+    n = eng.n
+    L = native.lib()
+    st = torch.cuda.current_stream(dev).cuda_stream
+    inv = ws.inverses(0.85)
+    gen = torch.Generator(device=dev).manual_seed(0)
+    T = torch.rand((n, K), generator=gen, device=dev)
+    Y = torch.empty_like(T)
+    nf = torch.zeros_like(T)
+    part = torch.zeros((ws.windows, K), device=dev)
+
+    def apply():
+        native.check(L.gl_window_apply(inv.data_ptr(), n, K, T.data_ptr(), 0.85, Y.data_ptr(), nf.data_ptr(),
+                                       0.15, 0, part.data_ptr(), st))
+
+    def spmm():
+        ws.off.spmm(T, Y)
+
+    out = {}
+    for name, fn in (("window_apply", apply), ("off_window_spmm", spmm)):
+        fn()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        out[name] = {"ms": round(e0.elapsed_time(e1) / reps, 4)}
+    W = ws.windows
+    apply_bytes = W * 64 * 64 * 4 + 4 * n * K * 4 + 2 * W * K * 4
+    ms = out["window_apply"]["ms"]
+    out["window_apply"].update({"alg_bytes": apply_bytes, "alg_GBs": round(apply_bytes / ms / 1e6, 1),
+                                "gflop": round(2 * 64 * n * K / 1e9, 2),
+                                "tflops": round(2 * 64 * n * K / ms / 1e9, 2)})
+    nnz = ws.off.nnz
+    sp_bytes = 8 * nnz + 4 * (n + 1) + 8 * n * K
+    out["off_window_spmm"].update({"nnz": nnz, "alg_bytes": sp_bytes,
+                                   "alg_GBs": round(sp_bytes / out["off_window_spmm"]["ms"] / 1e6, 1)})
+    out["columns"] = K
+    return out
 
 
 def serving(device, rates=(200.0, 800.0, 3200.0), requests_per_rate: int = 400, graphs: int = 8,
             seed: int = 5) -> dict:
-    """The serving configuration with the learned warm start on (as the
+    """The serving configuration with the warm start on (as the
     configuration asks) and, for comparison, off."""
     on = serving_pass(device, rates, requests_per_rate, graphs, True, seed)
     off = serving_pass(device, rates, requests_per_rate, graphs, False, seed)
     return {"workload": on["workload"].replace(", warm start on", ""), "resident_bytes": on["resident_bytes"],
-            "warm_start_on": {"rates": on["rates"], "admission_waits": on["admission_waits"]},
+            "warm_start_on": {"start": on.get("warm_start"), "setup_s": on.get("warm_setup_s"),
+                              "rates": on["rates"], "admission_waits": on["admission_waits"],
+                              "gates": on.get("warm_gates")},
             "warm_start_off": {"rates": off["rates"], "admission_waits": off["admission_waits"]}}
 
 
@@ -135,25 +296,25 @@ def serving_pass(device, rates=(200.0, 800.0, 3200.0), requests_per_rate: int = 
     Poisson arrivals at each rate, 1-64 seeds per request, alpha in
     {0.8, 0.85, 0.9}, certified L1 1e-6; p50 / p99 latency and queries/s."""
     from .serving import PPRServer, latency_summary
-    from .warmstart import WarmStart, WarmStartGate
+    from .warmstart import WarmStartGate
+    from .window_start import WindowStart
     rng = np.random.default_rng(seed)
     sizes = np.sort(np.round(rng.uniform(16, 22, graphs)).astype(int))
     srv = PPRServer(device=device, chunk=8)
     descr = []
-    ws_model = None
-    if warm:
-        gt = synth.cluster_zipf_graph(log2n=16, mean_degree=20.0, seed=99)
-        et = PPREngine(gt.A, block_size=8, min_nnz_per_block=4, device=device, dangling=gt.dangling)
-        ws_model = WarmStart(et, seed=0)
-        ws_model.train(num_vectors=4096, batch=256, nodes_per_vector=512, epochs=6)
+    setup_s = 0.0
     for i, lg in enumerate(sizes):
         g = synth.cluster_zipf_graph(log2n=int(lg), mean_degree=20.0, seed=200 + i, device=device)
         eng = srv.add_graph(f"g{i}", g.A, dangling=g.dangling, block_size=8, min_nnz=4)
-        if ws_model is not None:
-            # one model for the whole graph class; each graph's gate keeps the
-            # prediction only where it saves more than it costs
-            w = WarmStart(eng, seed=0, gate=WarmStartGate())
-            w.mlp = ws_model.mlp
+        if warm:
+            # window-solve start per graph; its gate keeps it only while the
+            # iterations it saves outweigh its cost.  The per-alpha window
+            # inverses and far-field shapes are built here, before the clock.
+            t0 = time.perf_counter()
+            w = WindowStart(eng, leaves=3, gate=WarmStartGate())
+            for a in (0.8, 0.85, 0.9):
+                w.inverses(a)
+            setup_s += time.perf_counter() - t0
             srv.warm[f"g{i}"] = w
         descr.append(int(g.n))
     # warm up every graph once
@@ -163,6 +324,9 @@ def serving_pass(device, rates=(200.0, 800.0, 3200.0), requests_per_rate: int = 
     out = {"workload": f"serving: {graphs} cluster/Zipf graphs, n = {descr}, Poisson arrivals, 1-64 seeds, "
                        f"alpha in {{.8,.85,.9}}, certified L1 1e-6, warm start {'on' if warm else 'off'}",
            "resident_bytes": srv.resident_bytes(), "rates": []}
+    if warm:
+        out["warm_start"] = "window-solve start (3 window exits, expected far field), per-graph gate"
+        out["warm_setup_s"] = round(setup_s, 2)
     srv.start()
     try:
         for lam in rates:
