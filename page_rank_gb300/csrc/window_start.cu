@@ -104,104 +104,181 @@ struct ApplyArgs {
     const float* T;        // [n][K]
     float* Y;              // [n][K] or null
     float* nf;             // near field [n][K] or null
-    float* partial;        // [windows][K] column sums of near_scale * Y per window
+    float* partial;        // [windows][K] column sums of near_scale * Y per window, or null
     int64_t n;
     int K;
     float scale;           // Y = scale * inv_w T_w
     float near_scale;      // nf (+)= near_scale * Y
     int near_init;         // 1: nf = ..., partial = ...; 0: nf += ..., partial += ...
-    int vec;               // K % 4 == 0 and every row pointer 16-byte aligned
+    int vec;               // K % 4 == 0 and T / Y / nf 16-byte aligned
 };
 
-// Y_w = scale * inv_w @ T_w for every window w and column tile of 64; the
-// window's inverse is held transposed in shared memory, each thread owns a
-// 4 x 4 patch of the output tile.
-__global__ void __launch_bounds__(kThreads) window_apply_kernel(ApplyArgs a, int64_t windows) {
-    __shared__ __align__(16) float invT[kWin * kLd];   // invT[q][r] = inv[r][q]
-    __shared__ __align__(16) float Ts[kWin * kLd];     // Ts[q][c]   = T[row0 + q][c0 + c]
-    __shared__ float red[16 * kWin];
-    const int t = threadIdx.x, rg = t >> 4, cg = t & 15;
+// Thread layout of the apply for a column tile of TW columns: 128 threads as
+// RG row groups x CG column groups; a thread owns RM rows x CN columns of the
+// 64 x TW output tile (with CN = 8 its columns are two runs of four, cg * 4
+// and TW / 2 + cg * 4, so a warp's shared-memory reads stay contiguous).
+constexpr int kApplyThreads = 128;
+template <int TW>
+struct ApplyShape {
+    static constexpr int CN = TW >= 128 ? 8 : 4;
+    static constexpr int CG = TW / CN;
+    static constexpr int RG = kApplyThreads / CG;
+    static constexpr int RM = kWin / RG;
+    static constexpr int LDT = TW + 4;                 // padded tile row (floats)
+    static constexpr int SMEM = (kWin * kLd + kWin * LDT) * 4;
+    static_assert(CG * CN == TW && RG * CG == kApplyThreads && RM * RG == kWin, "layout");
+    static_assert(RG * TW <= kWin * LDT, "column sums fit in the tile");
+};
+
+template <int RM>
+__device__ __forceinline__ void load_rows(const float* p, float (&a)[RM]) {
+    if constexpr (RM % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < RM; i += 4) {
+            const float4 v = *reinterpret_cast<const float4*>(p + i);
+            a[i] = v.x; a[i + 1] = v.y; a[i + 2] = v.z; a[i + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < RM; ++i) a[i] = p[i];
+    }
+}
+
+// Y_w = scale * inv_w @ T_w for every window w and column tile of TW: the
+// window's inverse is held transposed in shared memory (invT[q][r]), the
+// T tile beside it; each thread accumulates its RM x CN patch over the 64
+// rows q of the window, then writes Y / the near field and the tile's
+// per-window column sums.
+template <int TW>
+__global__ void __launch_bounds__(kApplyThreads, 4) window_apply_kernel(ApplyArgs a, int64_t windows) {
+    using S = ApplyShape<TW>;
+    constexpr int RM = S::RM, CN = S::CN, CG = S::CG, RG = S::RG, LDT = S::LDT;
+    extern __shared__ __align__(16) float smem[];
+    float* invT = smem;                    // [64][kLd]
+    float* Ts = smem + kWin * kLd;         // [64][LDT]; reused for the column sums
+    const int t = threadIdx.x, rg = t / CG, cg = t % CG;
     const int64_t K = a.K;
+    int cols[CN];
+#pragma unroll
+    for (int j = 0; j < CN; ++j) cols[j] = (CN == 8 && j >= 4) ? TW / 2 + cg * 4 + (j - 4) : cg * 4 + (j & 3);
     for (int64_t w = blockIdx.x; w < windows; w += gridDim.x) {
         const float* g = a.inv + w * kBlk;
         const int64_t row0 = w * kWin;
         const int rows = (int)min((int64_t)kWin, a.n - row0);
         __syncthreads();                                   // the previous window is done with invT
-        for (int i = t; i < kBlk; i += kThreads) invT[(i & 63) * kLd + (i >> 6)] = g[i];
-        for (int64_t c0 = 0; c0 < K; c0 += kWin) {
-            const int tw = (int)min((int64_t)kWin, K - c0);
-            __syncthreads();                               // Ts and red are free
-            if (a.vec && tw == kWin) {
-                for (int i = t; i < kWin * 16; i += kThreads) {
-                    const int q = i >> 4, c4 = (i & 15) * 4;
+        for (int i = t; i < kBlk; i += kApplyThreads) invT[(i & 63) * kLd + (i >> 6)] = g[i];
+        for (int64_t c0 = 0; c0 < K; c0 += TW) {
+            const int tw = (int)min((int64_t)TW, K - c0);
+            __syncthreads();                               // Ts is free, invT is written
+            if (a.vec && tw == TW) {
+                constexpr int F4 = TW / 4;
+                for (int i = t; i < kWin * F4; i += kApplyThreads) {
+                    const int q = i / F4, c4 = (i % F4) * 4;
                     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (q < rows) v = *reinterpret_cast<const float4*>(a.T + (row0 + q) * K + c0 + c4);
-                    *reinterpret_cast<float4*>(Ts + q * kLd + c4) = v;
+                    *reinterpret_cast<float4*>(Ts + q * LDT + c4) = v;
                 }
             } else {
-                for (int i = t; i < kBlk; i += kThreads) {
-                    const int q = i >> 6, c = i & 63;
-                    Ts[q * kLd + c] = (q < rows && c < tw) ? a.T[(row0 + q) * K + c0 + c] : 0.0f;
+                for (int i = t; i < kWin * TW; i += kApplyThreads) {
+                    const int q = i / TW, c = i % TW;
+                    Ts[q * LDT + c] = (q < rows && c < tw) ? a.T[(row0 + q) * K + c0 + c] : 0.0f;
                 }
             }
             __syncthreads();
-            float acc[4][4] = {};
-#pragma unroll 8
+            float acc[RM][CN];
+#pragma unroll
+            for (int i = 0; i < RM; ++i)
+#pragma unroll
+                for (int j = 0; j < CN; ++j) acc[i][j] = 0.f;
+#pragma unroll 4
             for (int q = 0; q < kWin; ++q) {
-                const float4 av = *reinterpret_cast<const float4*>(invT + q * kLd + rg * 4);
-                const float4 bv = *reinterpret_cast<const float4*>(Ts + q * kLd + cg * 4);
-                const float ar[4] = {av.x, av.y, av.z, av.w};
-                const float br[4] = {bv.x, bv.y, bv.z, bv.w};
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(ar[i], br[j], acc[i][j]);
-            }
-            float csum[4] = {0.f, 0.f, 0.f, 0.f};
-            const int cb = cg * 4;
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const int r = rg * 4 + i;
-                if (r >= rows) continue;
-                const int64_t base = (row0 + r) * K + c0 + cb;
-                float y[4], nv[4];
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    y[j] = a.scale * acc[i][j];
-                    nv[j] = a.near_scale * y[j];
+                float ar[RM];
+                load_rows<RM>(invT + q * kLd + rg * RM, ar);
+                float br[CN];
+                const float4 b0 = *reinterpret_cast<const float4*>(Ts + q * LDT + cg * 4);
+                br[0] = b0.x; br[1] = b0.y; br[2] = b0.z; br[3] = b0.w;
+                if constexpr (CN == 8) {
+                    const float4 b1 = *reinterpret_cast<const float4*>(Ts + q * LDT + TW / 2 + cg * 4);
+                    br[4] = b1.x; br[5] = b1.y; br[6] = b1.z; br[7] = b1.w;
                 }
-                if (a.vec && cb + 3 < tw) {
-                    if (a.Y) *reinterpret_cast<float4*>(a.Y + base) = make_float4(y[0], y[1], y[2], y[3]);
-                    if (a.nf) {
-                        float4 o = a.near_init ? make_float4(0.f, 0.f, 0.f, 0.f)
-                                               : *reinterpret_cast<const float4*>(a.nf + base);
-                        o.x += nv[0]; o.y += nv[1]; o.z += nv[2]; o.w += nv[3];
-                        *reinterpret_cast<float4*>(a.nf + base) = o;
-                    }
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) csum[j] += nv[j];
-                } else {
+                for (int i = 0; i < RM; ++i)
+#pragma unroll
+                    for (int j = 0; j < CN; ++j) acc[i][j] = fmaf(ar[i], br[j], acc[i][j]);
+            }
+            float csum[CN];
+#pragma unroll
+            for (int j = 0; j < CN; ++j) csum[j] = 0.f;
+#pragma unroll
+            for (int i = 0; i < RM; ++i) {
+                const int r = rg * RM + i;
+                if (r >= rows) continue;
+                const int64_t base = (row0 + r) * K + c0;
+#pragma unroll
+                for (int h = 0; h < CN; h += 4) {
+                    const int cb = cols[h];
+                    float y[4], nv[4];
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
-                        if (cb + j >= tw) continue;
-                        if (a.Y) a.Y[base + j] = y[j];
-                        if (a.nf) a.nf[base + j] = a.near_init ? nv[j] : a.nf[base + j] + nv[j];
-                        csum[j] += nv[j];
+                        y[j] = a.scale * acc[i][h + j];
+                        nv[j] = a.near_scale * y[j];
+                    }
+                    if (a.vec && cb + 3 < tw) {
+                        if (a.Y) *reinterpret_cast<float4*>(a.Y + base + cb) = make_float4(y[0], y[1], y[2], y[3]);
+                        if (a.nf) {
+                            float4 o = a.near_init ? make_float4(0.f, 0.f, 0.f, 0.f)
+                                                   : *reinterpret_cast<const float4*>(a.nf + base + cb);
+                            o.x += nv[0]; o.y += nv[1]; o.z += nv[2]; o.w += nv[3];
+                            *reinterpret_cast<float4*>(a.nf + base + cb) = o;
+                        }
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) csum[h + j] += nv[j];
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            if (cb + j >= tw) continue;
+                            if (a.Y) a.Y[base + cb + j] = y[j];
+                            if (a.nf) a.nf[base + cb + j] = a.near_init ? nv[j] : a.nf[base + cb + j] + nv[j];
+                            csum[h + j] += nv[j];
+                        }
                     }
                 }
             }
+            if (a.partial) {
+                __syncthreads();                           // every thread is done reading Ts
 #pragma unroll
-            for (int j = 0; j < 4; ++j) red[rg * kWin + cb + j] = csum[j];
-            __syncthreads();
-            if (t < tw && a.partial) {
-                float s = 0.f;
-#pragma unroll
-                for (int r = 0; r < 16; ++r) s += red[r * kWin + t];
-                float* p = a.partial + w * K + c0 + t;
-                *p = a.near_init ? s : *p + s;
+                for (int j = 0; j < CN; ++j) Ts[rg * TW + cols[j]] = csum[j];
+                __syncthreads();
+                for (int c = t; c < tw; c += kApplyThreads) {
+                    float sum = 0.f;
+#pragma unroll 8
+                    for (int r = 0; r < RG; ++r) sum += Ts[r * TW + c];
+                    float* p = a.partial + w * K + c0 + c;
+                    *p = a.near_init ? sum : *p + sum;
+                }
             }
         }
     }
+}
+
+template <int TW>
+int launch_apply(const ApplyArgs& a, int64_t windows, cudaStream_t stream) {
+    using S = ApplyShape<TW>;
+    static std::atomic<int> attr_cache[kMaxDevices];
+    int attr = 0;
+    const int rc = per_device_value(
+        attr_cache,
+        [&](int* v) {
+            GL_CUDA_TRY(cudaFuncSetAttribute(window_apply_kernel<TW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             S::SMEM));
+            *v = 1;
+            return GL_OK;
+        },
+        &attr);
+    if (rc != GL_OK) return rc;
+    window_apply_kernel<TW><<<grid_for(windows, 4), kApplyThreads, S::SMEM, stream>>>(a, windows);
+    GL_LAUNCH_CHECK("window_apply_kernel");
+    return GL_OK;
 }
 
 // colpart[y][c] = sum of partial[w][c] over the windows w of slice y;
@@ -370,9 +447,12 @@ extern "C" int gl_window_apply(const float* inverses, int64_t n, int32_t K, cons
     a.near_init = near_init ? 1 : 0;
     a.vec = (K % 4 == 0) && al16(T) && al16(Y) && al16(near_field);
     const int64_t windows = ceil_div(n, kWin);
-    window_apply_kernel<<<grid_for(windows, 6), kThreads, 0, stream>>>(a, windows);
-    GL_LAUNCH_CHECK("window_apply_kernel");
-    return GL_OK;
+    // column tile: the widest of 128 / 64 / 32 / 16 / 8 that K fills
+    if (K >= 128) return launch_apply<128>(a, windows, stream);
+    if (K >= 64) return launch_apply<64>(a, windows, stream);
+    if (K >= 32) return launch_apply<32>(a, windows, stream);
+    if (K >= 16) return launch_apply<16>(a, windows, stream);
+    return launch_apply<8>(a, windows, stream);
 }
 
 namespace {

@@ -404,12 +404,11 @@ class FarFieldModel:
         for c0 in range(0, len(seed_sets), batch):
             sl = seed_sets[c0:c0 + batch]
             res = eng.solve(sl, alpha=alpha, tol=tol)
-            V = eng.teleport_columns(sl)
-            near, _ = ws._near_field(V, alpha, keep_v=False)
+            near = ws.near_field(sl, alpha)
             far = (res.X - near).clamp_min(0)
             far = far / far.sum(dim=0, keepdim=True).clamp_min(1e-30)
             acc += far.sum(dim=1, dtype=torch.float64)
-            del far, near, V, res
+            del far, near, res
         target_mass = (acc / max(1, len(seed_sets))).to(torch.float32)   # [n], sums to 1
         T = torch.log(n * target_mass + 1e-6)
         F = self.features(ws, alpha)

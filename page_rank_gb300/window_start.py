@@ -46,6 +46,10 @@ from .ppr import PprRun, teleport_from_seed_sets
 
 WINDOW = 64
 SHAPES = ("expected", "pagerank", "learned")
+# window exits the start follows by default: on the cluster / Zipf class the
+# wall time of a 256-query batch fell up to 8 (2**21 nodes: 0.280 s cold,
+# 0.084 s from the start with 8 exits)
+DEFAULT_LEAVES = 8
 
 
 def _stream(dev) -> int:
@@ -95,7 +99,7 @@ class WindowStart:
     built on first use and kept; ``leaves`` is the number of times the
     series follows the edges that leave a window."""
 
-    def __init__(self, engine: PPREngine, leaves: int = 3, shape: str = "expected", gate=None,
+    def __init__(self, engine: PPREngine, leaves: int = DEFAULT_LEAVES, shape: str = "expected", gate=None,
                  fallback: bool = True, far_field_model=None):
         if shape not in SHAPES:
             raise ValueError(f"shape must be one of {SHAPES}")
@@ -187,9 +191,7 @@ class WindowStart:
         """(near field of the uniform teleport vector, its far field: PageRank
         minus that near field, normalized; non-negative up to rounding)."""
         n = self.eng.n
-        u = torch.full((n, 1), 1.0 / n, dtype=torch.float32, device=self.dev)
-        near, _ = self._near_field(u, alpha)
-        near = near[:, 0].contiguous()
+        near = self.near_field([np.arange(n)], alpha)[:, 0].contiguous()
         far = (pagerank - near).clamp_min(0)
         tot = far.sum()
         if not bool(tot > 0):
@@ -197,38 +199,63 @@ class WindowStart:
         return near, (far / tot).contiguous()
 
     # -- start vectors ------------------------------------------------------------
-    def _near_field(self, V: torch.Tensor, alpha: float, keep_v: bool = True):
+    def _teleport(self, seed_sets, tel: tuple | None = None):
+        """(teleport index, stripe-indexed teleport, dense teleport columns)."""
+        eng = self.eng
+        tel = eng.teleport(seed_sets) if tel is None else tel
+        ptr, rows, w = tel
+        tp = teleport_from_seed_sets(ptr, rows, eng.n, eng.block_size, w)
+        return tel, tp, eng.teleport_columns(seed_sets, tel)
+
+    def _near_field(self, V: torch.Tensor, tp, alpha: float):
         """(near field [n, K], per-window column sums [windows, K]) of the
-        columns of V, following ``leaves`` window exits."""
+        teleport columns V.
+
+        The series is summed term by term: y_0 = B^-1 v, then ``leaves``
+        times T = M y (the off-window SpMM) and y = alpha B^-1 T, each term
+        added into the near field as it is made (one fused apply).  Summing
+        the terms keeps the rounding of the large early terms out of the
+        later ones; re-solving the whole near field in every sweep (the
+        equivalent block-Jacobi iteration nf <- B^-1 (alpha M nf + (1 - alpha)
+        v)) put FP32 rounding of the full vector into each sweep and needed
+        two more certification steps at 8 exits on the 2**21-node graph.
+        ``tp`` (the same vectors, stripe-indexed) is not needed here."""
         st = self._prepare(alpha)
         L = native.lib()
         s = _stream(self.dev)
         n, K = V.shape
         inv = st["inv"]
-        nf = torch.empty_like(V)
-        Y = torch.empty_like(V)
-        partial = torch.empty((self.windows, K), dtype=torch.float32, device=self.dev)
         a = float(alpha)
-        native.check(L.gl_window_apply(inv.data_ptr(), n, K, V.data_ptr(), 1.0, Y.data_ptr(), nf.data_ptr(),
-                                       1.0 - a, 1, partial.data_ptr(), s))
-        T = V if not keep_v else torch.empty_like(V)
-        for k in range(1, self.leaves + 1):
-            self.off.spmm(Y, T)
-            last = k == self.leaves
-            native.check(L.gl_window_apply(inv.data_ptr(), n, K, T.data_ptr(), a,
-                                           None if last else Y.data_ptr(), nf.data_ptr(), 1.0 - a, 0,
-                                           partial.data_ptr(), s))
+        nf = torch.empty_like(V)
+        partial = torch.empty((self.windows, K), dtype=torch.float32, device=self.dev)
+        Y = torch.empty_like(V) if self.leaves else None
+        native.check(L.gl_window_apply(inv.data_ptr(), n, K, V.data_ptr(), 1.0,
+                                       Y.data_ptr() if Y is not None else None, nf.data_ptr(), 1.0 - a, 1,
+                                       partial.data_ptr(), s))
+        if self.leaves:
+            T = torch.empty_like(V)
+            for k in range(1, self.leaves + 1):
+                self.off.spmm(Y, T)
+                last = k == self.leaves
+                native.check(L.gl_window_apply(inv.data_ptr(), n, K, T.data_ptr(), a,
+                                               None if last else Y.data_ptr(), nf.data_ptr(), 1.0 - a, 0,
+                                               partial.data_ptr(), s))
         return nf, partial
+
+    def near_field(self, seed_sets, alpha: float) -> torch.Tensor:
+        """The exact truncated series (no far field) for the seed sets [n, K]."""
+        _, tp, V = self._teleport(seed_sets)
+        return self._near_field(V, tp, alpha)[0]
 
     def start(self, seed_sets, alpha: float = 0.85) -> torch.Tensor:
         """Window-start columns [n, K] (each sums to 1) for the seed sets."""
         st = self._prepare(alpha)
-        V = self.eng.teleport_columns(seed_sets)
-        return self._start_from(V, st, keep_v=False)
+        _, tp, V = self._teleport(seed_sets)
+        return self._start_from(V, st, tp)
 
-    def _start_from(self, V: torch.Tensor, st: dict, keep_v: bool) -> torch.Tensor:
+    def _start_from(self, V: torch.Tensor, st: dict, tp) -> torch.Tensor:
         n, K = V.shape
-        nf, partial = self._near_field(V, st["alpha"], keep_v=keep_v)
+        nf, partial = self._near_field(V, tp, st["alpha"])
         nbytes = native.lib().gl_window_finalize_workspace_bytes(n, K)
         ws = torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=self.dev)
         native.check(native.lib().gl_window_finalize(nf.data_ptr(), n, K, partial.data_ptr(),
@@ -289,14 +316,12 @@ class WindowStart:
         if self.gate is not None:
             ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
             ev[0].record()
-        V = eng.teleport_columns(seed_sets, tel)
-        x0 = self._start_from(V, st, keep_v=True)
+        tel, tp, V = self._teleport(seed_sets, tel)
+        x0 = self._start_from(V, st, tp)
         if ev is not None:
             ev[1].record()
         if not self.fallback:
             return x0, np.ones(k, dtype=bool)
-        ptr, rows, w = tel
-        tp = teleport_from_seed_sets(ptr, rows, eng.n, eng.block_size, w)
         run = PprRun(eng.meta, eng.n, eng.n, eng.block_size, eng.block_size, tp, alpha, 1, 0.0,
                      native.GL_PPR_STOP_ALL, eng.dbits)
         run.init(x0)

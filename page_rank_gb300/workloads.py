@@ -125,7 +125,7 @@ def ppr_step(device, log2n: int = 22, K: int = 256, block: int = 4, min_nnz: int
             "alg_GBs": round(B / ms / 1e6, 1)}
 
 
-def warmstart(device, log2n: int = 21, train_vectors: int = 20000, K: int = 256, leaves=(2, 3, 4, 6, 8),
+def warmstart(device, log2n: int = 21, train_vectors: int = 20000, K: int = 256, leaves=(2, 4, 6, 8, 10),
               layout=(4, 4, 0), mlp_start: bool = True, keep_x: bool = False) -> dict:
     """Warm starts on the cluster / Zipf graph class at n = 2**log2n, K held-out
     seed sets of 1-32 seeds, alpha 0.85, certified L1 1e-6, each solved cold
@@ -147,10 +147,11 @@ def warmstart(device, log2n: int = 21, train_vectors: int = 20000, K: int = 256,
     bs, mn, ct = layout
     eng = PPREngine(g.A, block_size=bs, min_nnz_per_block=mn, device=device, dangling=g.dangling, column_tile=ct)
     sets = synth.seed_sets(g.n, K, 1, 32, seed=424242)
-    eng.solve(sets[:8], alpha=alpha, tol=tol)
-    torch.cuda.synchronize(device)
 
     def timed(fn):
+        # one untimed run first (allocations at this width, launch shapes),
+        # then the timed one: every variant is measured the same way
+        fn()
         torch.cuda.synchronize(device)
         t0 = time.perf_counter()
         r = fn()
@@ -173,14 +174,17 @@ def warmstart(device, log2n: int = 21, train_vectors: int = 20000, K: int = 256,
                        f"certified L1 {tol:g}, PBR {bs}x{bs} min {mn}",
            "n": g.n, "nnz": int(g.A.nnz), "cold": record(cold, t_cold), "starts": {}}
     ws = WindowStart(eng, leaves=max(leaves), shape="pagerank")
-    _, setup = timed(lambda: ws.inverses(alpha))
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    ws.inverses(alpha)                          # inverses, PageRank, far field: once per graph and alpha
+    torch.cuda.synchronize(device)
+    setup = time.perf_counter() - t0
     out["window_setup_s"] = round(setup, 3)
     out["off_window_nnz"] = ws.off.nnz
     best = None
     for L in leaves:
         ws.leaves = L
         ws.set_shape("expected")
-        ws.solve(sets[:8], alpha=alpha, tol=tol)
         res, t = timed(lambda: ws.solve(sets, alpha=alpha, tol=tol))
         _, t_start = timed(lambda: ws.start(sets, alpha))
         rec = record(res, t)
@@ -228,11 +232,13 @@ def warmstart(device, log2n: int = 21, train_vectors: int = 20000, K: int = 256,
 
 
 def window_start_kernels(ws, K: int, reps: int = 5) -> dict:
-    """CUDA-event times of the window start's two kernels on K columns:
-    ``gl_window_apply`` (accumulating, with Y) and the off-window SpMM.
-    Algorithmic bytes of one apply: the inverses (16 KB per window), T read,
-    Y written, the near field read and written, the per-window sums read
-    and written; FLOPs 2 * 64 per output entry."""
+    """CUDA-event times of the window start's two kernels over K columns, as
+    one window exit runs them: the off-window SpMM (``gl_pbr_spmm`` over M)
+    and ``gl_window_apply`` (y = alpha B^-1 T written, added into the near
+    field, per-window column sums updated).  Algorithmic bytes: the SpMM
+    reads M (8 bytes per entry as CSR) and X and writes Y; the apply reads
+    the inverses (16 KB per window) and T, writes y, reads and writes the
+    near field and the column sums.  FLOPs of the apply: 2 * 64 per output."""
     eng = ws.eng
     dev = ws.dev
     n = eng.n
@@ -311,7 +317,7 @@ def serving_pass(device, rates=(200.0, 800.0, 3200.0), requests_per_rate: int = 
             # iterations it saves outweigh its cost.  The per-alpha window
             # inverses and far-field shapes are built here, before the clock.
             t0 = time.perf_counter()
-            w = WindowStart(eng, leaves=3, gate=WarmStartGate())
+            w = WindowStart(eng, gate=WarmStartGate())
             for a in (0.8, 0.85, 0.9):
                 w.inverses(a)
             setup_s += time.perf_counter() - t0
@@ -325,7 +331,7 @@ def serving_pass(device, rates=(200.0, 800.0, 3200.0), requests_per_rate: int = 
                        f"alpha in {{.8,.85,.9}}, certified L1 1e-6, warm start {'on' if warm else 'off'}",
            "resident_bytes": srv.resident_bytes(), "rates": []}
     if warm:
-        out["warm_start"] = "window-solve start (3 window exits, expected far field), per-graph gate"
+        out["warm_start"] = "window-solve start (8 window exits, expected far field), per-graph gate"
         out["warm_setup_s"] = round(setup_s, 2)
     srv.start()
     try:

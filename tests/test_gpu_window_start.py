@@ -60,7 +60,7 @@ def test_window_invert_reports_a_bad_pivot(device):
     assert status == 1
 
 
-@pytest.mark.parametrize("K", [1, 3, 64, 100, 256])
+@pytest.mark.parametrize("K", [1, 3, 8, 16, 40, 64, 100, 130, 256])
 @pytest.mark.parametrize("n", [130, 4096])
 def test_window_apply_matches_oracle(K, n, device):
     from page_rank_gb300 import native
@@ -166,7 +166,7 @@ def test_fallback_to_cold_start(device, monkeypatch):
     ws = WindowStart(eng, leaves=1)
     sets = synth.seed_sets(g.n, 6, 1, 8, seed=4)
 
-    def far_away(V, st, keep_v):              # all mass on one node far from every seed
+    def far_away(V, st, tp):                  # all mass on one node far from every seed
         X = torch.zeros_like(V)
         X[g.n - 1] = 1.0
         return X

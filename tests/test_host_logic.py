@@ -135,3 +135,10 @@ def test_warm_start_gate_keeps_prediction_only_when_it_pays():
     g2 = WarmStartGate(smoothing=0.0)
     g2.record(0.001, 0.002, 1, np.array([2.0]), np.array([1.0]))
     assert g2.saved_iters == 0.0 and not g2.want_prediction()
+
+
+def test_cpulist_parsing():
+    from page_rank_gb300.hostmem import _parse_cpulist, restore_cpus
+    assert _parse_cpulist("0-3,8,10-11\n") == [0, 1, 2, 3, 8, 10, 11]
+    assert _parse_cpulist("") == []
+    restore_cpus({"bound": False})          # nothing recorded: no change
