@@ -699,7 +699,7 @@ def main():
     ap.add_argument("--log2n", type=int, default=None,
                     help="graph size (2**log2n nodes); default: the workload's configuration size")
     ap.add_argument("--workload", choices=["spmm", "ppr_small", "ppr_batched", "ppr_step", "warmstart", "serving",
-                                           "kernels", "edges"],
+                                           "kernels", "edges", "window_kernels"],
                     default="spmm",
                     help="spmm (default, the headline line) or a secondary PPR workload")
     args = ap.parse_args()
@@ -718,7 +718,8 @@ def main():
         dev = torch.device("cuda", local_rank)
         torch.cuda.set_device(dev)
         fn = getattr(workloads, args.workload)
-        default_log2n = {"ppr_batched": 22, "ppr_step": 22, "warmstart": 21, "kernels": 20, "edges": 20}
+        default_log2n = {"ppr_batched": 22, "ppr_step": 22, "warmstart": 21, "kernels": 20, "edges": 20,
+                         "window_kernels": 21}
         out = fn(dev) if args.workload in ("ppr_small", "serving") else \
             fn(dev, log2n=args.log2n if args.log2n is not None else default_log2n[args.workload])
         out = {"workload": args.workload, **out}

@@ -223,14 +223,19 @@ def normalize_transition_matrix(A_csr: sp.csr_matrix) -> sp.csr_matrix:
 # ---------------------------------------------------------------------------
 def run_personalized_pagerank(pbr_mat, source_nodes: torch.Tensor, alpha: float = 0.85,
                               max_iterations: int = 100, tolerance: float = 1e-6,
-                              return_history: bool = False):
+                              return_history: bool = False, warm_start: torch.Tensor | None = None):
     """Batched PPR by power iteration (``__init__.py:210-271``):
 
         X_{t+1} = alpha * A @ X_t + (1 - alpha) * e_s
 
     one column per source node.  Stops when the largest per-column L1 update
     falls below ``tolerance``.  Returns ``(X, iterations, converged)`` or, with
-    ``return_history``, ``(X, iterations, converged, history)``."""
+    ``return_history``, ``(X, iterations, converged, history)``.
+
+    ``warm_start`` (an addition; the reference always starts from the
+    one-hot sources): start columns [rows, K] on the matrix's device, e.g.
+    ``window_start.WindowStart(...).start(...)``; the fixed point and the
+    stop rule are unchanged."""
     meta = get_pbr_gpu_meta(pbr_mat)
     if meta is None:
         raise RuntimeError("PBRMatrix is not on GPU. Call .to('cuda') first.")
@@ -247,7 +252,11 @@ def run_personalized_pagerank(pbr_mat, source_nodes: torch.Tensor, alpha: float 
         tp = teleport_from_seed_sets(seed_ptr, seeds, N, pbr_mat.block_rows)
         run = PprRun(meta, N, pbr_mat.cols, pbr_mat.block_rows, pbr_mat.block_cols, tp, alpha,
                      max_iterations, tolerance, native.GL_PPR_STOP_ALL, None)
-        res = run.run(chunk=8)
+        if warm_start is not None:
+            if tuple(warm_start.shape) != (N, K):
+                raise ValueError(f"warm_start must be [{N}, {K}]")
+            warm_start = warm_start.to(device=device, dtype=run.bufs[0].dtype)
+        res = run.run(chunk=8, x0=warm_start)
     if return_history:
         return res.X, res.iterations, res.converged, res.history
     return res.X, res.iterations, res.converged

@@ -283,6 +283,18 @@ def window_start_kernels(ws, K: int, reps: int = 5) -> dict:
     return out
 
 
+def window_kernels(device, log2n: int = 21, K: int = 256) -> dict:
+    """The window start's two kernels alone (``window_start_kernels``) on the
+    warm-start configuration's graph class at n = 2**log2n, K columns."""
+    from .window_start import WindowStart
+    g = synth.cluster_zipf_graph(log2n=log2n, mean_degree=20.0, seed=3, device=device)
+    eng = PPREngine(g.A, block_size=4, min_nnz_per_block=4, device=device, dangling=g.dangling)
+    ws = WindowStart(eng)
+    ws.inverses(0.85)
+    return {"workload": f"window start kernels: {g.description}, K={K}", "n": g.n, "nnz": int(g.A.nnz),
+            **window_start_kernels(ws, K)}
+
+
 def serving(device, rates=(200.0, 800.0, 3200.0), requests_per_rate: int = 400, graphs: int = 8,
             seed: int = 5) -> dict:
     """The serving configuration with the warm start on (as the

@@ -202,3 +202,22 @@ def test_learned_far_field_gains_over_pagerank_far_field(device):
     assert learned.iterations.mean() < base.iterations.mean(), (learned.iterations.mean(), base.iterations.mean(),
                                                                expected.iterations.mean())
     assert (learned.X.double() - base.X.double()).abs().sum(dim=0).max().item() < 2e-6
+
+
+def test_run_personalized_pagerank_warm_start_argument(device):
+    """graph_link.run_personalized_pagerank(..., warm_start=X0): the same
+    fixed point from a given start, fewer iterations from a good one."""
+    from page_rank_gb300 import graph_link as gl
+    from page_rank_gb300.engine import PPREngine
+    from page_rank_gb300.window_start import WindowStart
+    g = _graph(12)
+    pbr = gl.csr_to_pbr(g.A, block_rows=4, block_cols=4, min_nnz_per_block=4).to(device)
+    src = torch.tensor([3, 700, 4000], dtype=torch.int32, device=device)
+    Xc, it_c, conv_c = gl.run_personalized_pagerank(pbr, src, tolerance=1e-7, max_iterations=500)
+    eng = PPREngine(g.A, block_size=4, device=device)
+    x0 = WindowStart(eng, leaves=4).start([[3], [700], [4000]], 0.85)
+    Xw, it_w, conv_w = gl.run_personalized_pagerank(pbr, src, tolerance=1e-7, max_iterations=500, warm_start=x0)
+    assert conv_c and conv_w and it_w < it_c
+    assert (Xc.double() - Xw.double()).abs().sum(dim=0).max().item() < 2e-6
+    with pytest.raises(ValueError):
+        gl.run_personalized_pagerank(pbr, src, warm_start=x0[:, :2])
