@@ -458,11 +458,14 @@ int gl_window_blocks(const int32_t* indptr, const int32_t* indices, const float*
 
 /* Inverts every block in place (Gauss-Jordan without pivoting, valid for
  * strictly column diagonally dominant blocks: columns of A summing to at
- * most 1).  *status (device int32) is set to 0, then to 1 if a pivot was
- * not positive and finite; the caller reads it after the stream. */
+ * most 1) and stores each inverse transposed: entry (r, q) of block w at
+ * blocks[w * 4096 + q * 64 + r].  *status (device int32) is set to 0, then
+ * to 1 if a pivot was not positive and finite; the caller reads it after
+ * the stream. */
 int gl_window_invert(float* blocks, int64_t n, int32_t* status, cudaStream_t stream);
 
-/* Y = scale * B^-1 T window by window (T, Y, near_field: [n][K] row-major
+/* Y = scale * B^-1 T window by window (inverses as gl_window_invert leaves
+ * them; T, Y, near_field: [n][K] row-major
  * FP32); near_field = near_scale * Y (near_init = 1) or += (near_init = 0),
  * and partial[w][K] = (or +=) the column sums of near_scale * Y over window w
  * (partial may be NULL).  Y or near_field may be NULL, not both. */

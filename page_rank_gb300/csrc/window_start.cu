@@ -32,7 +32,6 @@ namespace {
 constexpr int kWin = 64;          // window rows (and columns of a window block)
 constexpr int kBlk = kWin * kWin;
 constexpr int kThreads = 256;
-constexpr int kLd = kWin + 4;     // padded shared-memory row (floats), keeps float4 alignment
 
 inline unsigned grid_for(int64_t items, int per_sm) {
     const int64_t cap = (int64_t)num_sms() * per_sm;
@@ -69,7 +68,9 @@ __global__ void window_blocks_kernel(const int32_t* __restrict__ indptr, const i
 
 // In-place Gauss-Jordan inversion of each 64 x 64 block, one CTA per block
 // at a time.  Per pivot k: scale row k, eliminate column k from the other
-// rows, then write column k of the inverse.
+// rows, then write column k of the inverse.  The inverse is stored
+// transposed (element (r, q) at q * 64 + r), the layout the apply reads:
+// for each q, the 64 rows' coefficients are contiguous.
 __global__ void __launch_bounds__(kThreads) window_invert_kernel(float* __restrict__ blocks, int64_t windows,
                                                                  int32_t* __restrict__ status) {
     __shared__ float M[kWin][kWin + 1];
@@ -94,13 +95,13 @@ __global__ void __launch_bounds__(kThreads) window_invert_kernel(float* __restri
             if (t < kWin) M[t][k] = t == k ? piv : -M[t][k] * piv;
             __syncthreads();
         }
-        for (int i = t; i < kBlk; i += kThreads) g[i] = M[i >> 6][i & 63];
+        for (int i = t; i < kBlk; i += kThreads) g[i] = M[i & 63][i >> 6];
         if (bad && t == 0) atomicExch(status, 1);
     }
 }
 
 struct ApplyArgs {
-    const float* inv;      // [windows][64][64]
+    const float* inv;      // [windows][64 (q)][64 (r)]: the inverses, transposed
     const float* T;        // [n][K]
     float* Y;              // [n][K] or null
     float* nf;             // near field [n][K] or null
@@ -117,15 +118,33 @@ struct ApplyArgs {
 // RG row groups x CG column groups; a thread owns RM rows x CN columns of the
 // 64 x TW output tile (with CN = 8 its columns are two runs of four, cg * 4
 // and TW / 2 + cg * 4, so a warp's shared-memory reads stay contiguous).
+// Tuning (measured on the 2**21-node graph, 256 columns, one apply, same
+// box): 64-column tiles (8 x 4 patches) at 6 CTAs per SM 2.25 ms (2.27
+// without the row padding); 7 CTAs (register cap 72: a spill) 3.22 ms;
+// 32-column tiles at 8 CTAs 2.56 ms; 128-column tiles (8 x 8 patches, 123
+// registers, 4 CTAs) 2.70 ms; a cp.async double-buffered 128-column kernel
+// (2 CTAs) 3.46 ms, the same at 64 columns (3 CTAs) 2.81 ms: resident warps
+// matter more than overlapping one CTA's copies.
+#ifndef GL_WIN_APPLY_MAXTW
+#define GL_WIN_APPLY_MAXTW 64        // widest column tile used
+#endif
+#ifndef GL_WIN_APPLY_PAD
+#define GL_WIN_APPLY_PAD 4           // floats of padding per shared-memory row
+#endif
+#ifndef GL_WIN_APPLY_CTAS
+#define GL_WIN_APPLY_CTAS 6          // resident CTAs per SM for tiles of <= 64 columns
+#endif
 constexpr int kApplyThreads = 128;
+constexpr int kLdI = kWin + GL_WIN_APPLY_PAD;    // inverse row in shared memory (floats)
 template <int TW>
 struct ApplyShape {
     static constexpr int CN = TW >= 128 ? 8 : 4;
     static constexpr int CG = TW / CN;
     static constexpr int RG = kApplyThreads / CG;
     static constexpr int RM = kWin / RG;
-    static constexpr int LDT = TW + 4;                 // padded tile row (floats)
-    static constexpr int SMEM = (kWin * kLd + kWin * LDT) * 4;
+    static constexpr int LDT = TW + GL_WIN_APPLY_PAD;  // tile row (floats)
+    static constexpr int CTAS = TW >= 128 ? 4 : GL_WIN_APPLY_CTAS;
+    static constexpr int SMEM = (kWin * kLdI + kWin * LDT) * 4;
     static_assert(CG * CN == TW && RG * CG == kApplyThreads && RM * RG == kWin, "layout");
     static_assert(RG * TW <= kWin * LDT, "column sums fit in the tile");
 };
@@ -150,12 +169,13 @@ __device__ __forceinline__ void load_rows(const float* p, float (&a)[RM]) {
 // rows q of the window, then writes Y / the near field and the tile's
 // per-window column sums.
 template <int TW>
-__global__ void __launch_bounds__(kApplyThreads, 4) window_apply_kernel(ApplyArgs a, int64_t windows) {
+__global__ void __launch_bounds__(kApplyThreads, ApplyShape<TW>::CTAS) window_apply_kernel(ApplyArgs a,
+                                                                                          int64_t windows) {
     using S = ApplyShape<TW>;
     constexpr int RM = S::RM, CN = S::CN, CG = S::CG, RG = S::RG, LDT = S::LDT;
     extern __shared__ __align__(16) float smem[];
-    float* invT = smem;                    // [64][kLd]
-    float* Ts = smem + kWin * kLd;         // [64][LDT]; reused for the column sums
+    float* invT = smem;                    // [64 q][kLdI]: the inverse, transposed
+    float* Ts = smem + kWin * kLdI;        // [64][LDT]; reused for the column sums
     const int t = threadIdx.x, rg = t / CG, cg = t % CG;
     const int64_t K = a.K;
     int cols[CN];
@@ -166,7 +186,8 @@ __global__ void __launch_bounds__(kApplyThreads, 4) window_apply_kernel(ApplyArg
         const int64_t row0 = w * kWin;
         const int rows = (int)min((int64_t)kWin, a.n - row0);
         __syncthreads();                                   // the previous window is done with invT
-        for (int i = t; i < kBlk; i += kApplyThreads) invT[(i & 63) * kLd + (i >> 6)] = g[i];
+        for (int i = t * 4; i < kBlk; i += kApplyThreads * 4)
+            *reinterpret_cast<float4*>(invT + (i >> 6) * kLdI + (i & 63)) = *reinterpret_cast<const float4*>(g + i);
         for (int64_t c0 = 0; c0 < K; c0 += TW) {
             const int tw = (int)min((int64_t)TW, K - c0);
             __syncthreads();                               // Ts is free, invT is written
@@ -193,7 +214,7 @@ __global__ void __launch_bounds__(kApplyThreads, 4) window_apply_kernel(ApplyArg
 #pragma unroll 4
             for (int q = 0; q < kWin; ++q) {
                 float ar[RM];
-                load_rows<RM>(invT + q * kLd + rg * RM, ar);
+                load_rows<RM>(invT + q * kLdI + rg * RM, ar);
                 float br[CN];
                 const float4 b0 = *reinterpret_cast<const float4*>(Ts + q * LDT + cg * 4);
                 br[0] = b0.x; br[1] = b0.y; br[2] = b0.z; br[3] = b0.w;
@@ -276,7 +297,7 @@ int launch_apply(const ApplyArgs& a, int64_t windows, cudaStream_t stream) {
         },
         &attr);
     if (rc != GL_OK) return rc;
-    window_apply_kernel<TW><<<grid_for(windows, 4), kApplyThreads, S::SMEM, stream>>>(a, windows);
+    window_apply_kernel<TW><<<grid_for(windows, S::CTAS), kApplyThreads, S::SMEM, stream>>>(a, windows);
     GL_LAUNCH_CHECK("window_apply_kernel");
     return GL_OK;
 }
@@ -447,9 +468,9 @@ extern "C" int gl_window_apply(const float* inverses, int64_t n, int32_t K, cons
     a.near_init = near_init ? 1 : 0;
     a.vec = (K % 4 == 0) && al16(T) && al16(Y) && al16(near_field);
     const int64_t windows = ceil_div(n, kWin);
-    // column tile: the widest of 128 / 64 / 32 / 16 / 8 that K fills
-    if (K >= 128) return launch_apply<128>(a, windows, stream);
-    if (K >= 64) return launch_apply<64>(a, windows, stream);
+    // column tile: the widest of GL_WIN_APPLY_MAXTW / 64 / 32 / 16 / 8 that K fills
+    if (GL_WIN_APPLY_MAXTW >= 128 && K >= 128) return launch_apply<128>(a, windows, stream);
+    if (GL_WIN_APPLY_MAXTW >= 64 && K >= 64) return launch_apply<64>(a, windows, stream);
     if (K >= 32) return launch_apply<32>(a, windows, stream);
     if (K >= 16) return launch_apply<16>(a, windows, stream);
     return launch_apply<8>(a, windows, stream);

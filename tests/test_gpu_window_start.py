@@ -50,7 +50,7 @@ def test_window_inverses_match_numpy(n, alpha, device):
     inv, status = _inverses(A, alpha, device)
     assert status == 0
     ref = np.linalg.inv(ows.window_blocks(A, alpha))
-    got = inv.cpu().numpy().astype(np.float64)
+    got = inv.cpu().numpy().astype(np.float64).transpose(0, 2, 1)     # stored transposed
     assert np.abs(got - ref).max() <= 1e-5 * max(1.0, np.abs(ref).max())
 
 
@@ -60,13 +60,13 @@ def test_window_invert_reports_a_bad_pivot(device):
     assert status == 1
 
 
-@pytest.mark.parametrize("K", [1, 3, 8, 16, 40, 64, 100, 130, 256])
+@pytest.mark.parametrize("K", [1, 3, 8, 16, 40, 64, 100, 128, 130, 200, 256])
 @pytest.mark.parametrize("n", [130, 4096])
 def test_window_apply_matches_oracle(K, n, device):
     from page_rank_gb300 import native
     A = _graph(12).A[:n, :n]
     inv, _ = _inverses(A, 0.85, device)
-    inv_np = inv.cpu().numpy().astype(np.float64)
+    inv_np = inv.cpu().numpy().astype(np.float64).transpose(0, 2, 1)
     rng = np.random.default_rng(K + n)
     T = rng.random((n, K)).astype(np.float32)
     N0 = rng.random((n, K)).astype(np.float32)
