@@ -449,6 +449,7 @@ def run_ppr(dev, args) -> dict:
     # the warm-start configuration (2**21 nodes of the same class): cold and
     # every start on the same held-out seed sets
     layout = (tuned.block_size, tuned.min_nnz, tuned.column_tile)
+    warm_setup_phases = wst.setup_phases.get(round(PPR_ALPHA, 12))
     del wst
     torch.cuda.empty_cache()
     wcfg = workloads.warmstart(dev, log2n=args.warm_log2n, train_vectors=args.ppr_train_vectors, K=K,
@@ -465,7 +466,7 @@ def run_ppr(dev, args) -> dict:
                   "iterations_sum": int(rp.iterations.sum())},
         "batched_warm": {"queries_per_s": round(qps_w, 2), "seconds_including_start": round(rw.seconds, 4),
                          "start": f"window-solve start: {warm_leaves} window exits, expected far field, cold fallback",
-                         "setup_s": round(warm_setup_s, 2),
+                         "setup_s": round(warm_setup_s, 2), "setup_phases": warm_setup_phases,
                          "iterations_sum": int(rw.iterations.sum()), "column_steps": rw.column_steps,
                          "columns_using_start": float(np.mean(rw.warm_columns)),
                          "all_converged": bool(rw.converged.all())},

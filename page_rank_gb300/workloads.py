@@ -180,6 +180,7 @@ def warmstart(device, log2n: int = 21, train_vectors: int = 20000, K: int = 256,
     torch.cuda.synchronize(device)
     setup = time.perf_counter() - t0
     out["window_setup_s"] = round(setup, 3)
+    out["window_setup_phases"] = ws.setup_phases.get(round(float(alpha), 12))
     out["off_window_nnz"] = ws.off.nnz
     best = None
     for L in leaves:
