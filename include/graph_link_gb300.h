@@ -305,9 +305,14 @@ typedef struct gl_teleport {
  * seed of column k the weight 1/|S_k| (uniform personalization over the set;
  * the reference's one-seed-per-column case, init_ppr_sources_kernel at
  * kernels/ppr_kernel.cu:199-209, is |S_k| = 1).  Outputs: stripe_ptr
- * (num_stripes + 1), row/col/weight (num_seeds).  counter_scratch: device
- * int32[num_stripes + 1].  Errors: GL_ERR_INVALID_ARGUMENT for a seed outside
- * [0, rows) — checked on the device and reported after a stream sync. */
+ * (num_stripes + 1), row/col/weight (num_seeds); the order of the entries
+ * within a stripe is unspecified (each adds into its own (row, column)
+ * element, so results do not depend on it unless a (seed, column) pair
+ * repeats).  counter_scratch: device int32[num_stripes + 1].  seed_ptr must
+ * be non-decreasing with seed_ptr[0] = 0 and seed_ptr[num_columns] =
+ * num_seeds.  Errors: GL_ERR_INVALID_ARGUMENT for a seed outside [0, rows)
+ * or a seed_ptr that does not cover the seeds — checked on the device and
+ * reported after a stream sync. */
 int gl_ppr_teleport_index(int64_t rows, int32_t block_rows, int64_t num_columns,
                           const int32_t* seed_ptr, const int32_t* seed_idx,
                           const float* seed_weight, int64_t num_seeds,

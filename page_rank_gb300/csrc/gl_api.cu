@@ -211,14 +211,30 @@ __global__ void stripe_index_kernel(const int32_t* coords, int64_t nb, int64_t r
     for (int64_t s = s_prev + 1; s <= s_cur; ++s) ptr[s] = (int32_t)b;
 }
 
-__global__ void teleport_count_kernel(int64_t K, const int32_t* seed_ptr, const int32_t* seed_idx, int64_t rows,
-                                      int br, int32_t* counters, int64_t ns, int32_t* stripe_ptr, int32_t* row,
-                                      int32_t* col, float* weight, const float* seed_w, bool scatter) {
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= K) return;
-    const int32_t e0 = seed_ptr[k], e1 = seed_ptr[k + 1];
-    const float uni = e1 > e0 ? 1.0f / (float)(e1 - e0) : 0.0f;
-    for (int32_t e = e0; e < e1; ++e) {
+// One thread per seed entry (grid-stride): its column is found by binary
+// search in seed_ptr, so a column with millions of seeds (a uniform teleport
+// vector) is spread over the whole grid instead of one thread.  Pass 1
+// counts the entries of each stripe; pass 2 scatters them.  Slots within a
+// stripe come from atomics, so their order is unspecified; the step's
+// epilogue adds each entry to its own (row, column) element, so results do
+// not depend on it unless a (seed, column) pair repeats.
+__global__ void teleport_count_kernel(int64_t K, const int32_t* seed_ptr, const int32_t* seed_idx,
+                                      int64_t num_seeds, int64_t rows, int br, int32_t* counters, int64_t ns,
+                                      int32_t* stripe_ptr, int32_t* row, int32_t* col, float* weight,
+                                      const float* seed_w, bool scatter) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < num_seeds;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        int64_t lo = 0, hi = K;                 // last column k with seed_ptr[k] <= e
+        while (hi - lo > 1) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (seed_ptr[mid] <= e) lo = mid; else hi = mid;
+        }
+        const int64_t k = lo;
+        const int32_t e0 = seed_ptr[k], e1 = seed_ptr[k + 1];
+        if (e < e0 || e >= e1) {                // seed_ptr not covering [0, num_seeds)
+            atomicOr(&counters[ns], 2);
+            continue;
+        }
         const int64_t r = seed_idx[e];
         if (r < 0 || r >= rows) {
             atomicOr(&counters[ns], 1);
@@ -231,7 +247,7 @@ __global__ void teleport_count_kernel(int64_t K, const int32_t* seed_ptr, const 
             const int32_t slot = stripe_ptr[s] + atomicAdd(&counters[s], 1);
             row[slot] = (int32_t)r;
             col[slot] = (int32_t)k;
-            weight[slot] = seed_w ? seed_w[e] : uni;
+            weight[slot] = seed_w ? seed_w[e] : 1.0f / (float)(e1 - e0);
         }
     }
 }
@@ -440,16 +456,19 @@ extern "C" int gl_ppr_teleport_index(int64_t rows, int32_t block_rows, int64_t n
     GL_REQUIRE(stripe_ptr && counter_scratch, GL_ERR_INVALID_ARGUMENT, "NULL output");
     const int64_t ns = ceil_div(rows, block_rows);
     GL_CUDA_TRY(cudaMemsetAsync(counter_scratch, 0, sizeof(int32_t) * (ns + 1), stream));
-    const unsigned grid = (unsigned)ceil_div(num_columns > 0 ? num_columns : 1, 128);
-    if (num_columns > 0) {
-        teleport_count_kernel<<<grid, 128, 0, stream>>>(num_columns, seed_ptr, seed_idx, rows, block_rows,
-                                                        counter_scratch, ns, nullptr, nullptr, nullptr, nullptr,
-                                                        nullptr, false);
+    const int64_t work = num_columns > 0 ? num_seeds : 0;
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(work, 256),
+                                                                           (int64_t)num_sms() * 8));
+    if (work > 0) {
+        teleport_count_kernel<<<grid, 256, 0, stream>>>(num_columns, seed_ptr, seed_idx, num_seeds, rows,
+                                                        block_rows, counter_scratch, ns, nullptr, nullptr, nullptr,
+                                                        nullptr, nullptr, false);
         GL_LAUNCH_CHECK("teleport_count_kernel");
     }
     int32_t bad = 0;
     GL_CUDA_TRY(cudaMemcpyAsync(&bad, counter_scratch + ns, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
     GL_CUDA_TRY(cudaStreamSynchronize(stream));
+    GL_REQUIRE(!(bad & 2), GL_ERR_INVALID_ARGUMENT, "seed_ptr does not cover the %lld seeds", (long long)num_seeds);
     GL_REQUIRE(bad == 0, GL_ERR_INVALID_ARGUMENT, "seed node index out of range [0, %lld)", (long long)rows);
     // Per-stripe counts -> stripe_ptr (exclusive scan).  The counters are
     // free once copied, so they double as the scan's scratch (it needs at
@@ -462,10 +481,10 @@ extern "C" int gl_ppr_teleport_index(int64_t rows, int32_t block_rows, int64_t n
         if (rc != GL_OK) return rc;
     }
     GL_CUDA_TRY(cudaMemsetAsync(counter_scratch, 0, sizeof(int32_t) * (ns + 1), stream));
-    if (num_columns > 0) {
-        teleport_count_kernel<<<grid, 128, 0, stream>>>(num_columns, seed_ptr, seed_idx, rows, block_rows,
-                                                        counter_scratch, ns, stripe_ptr, row, col, weight,
-                                                        seed_weight, true);
+    if (work > 0) {
+        teleport_count_kernel<<<grid, 256, 0, stream>>>(num_columns, seed_ptr, seed_idx, num_seeds, rows,
+                                                        block_rows, counter_scratch, ns, stripe_ptr, row, col,
+                                                        weight, seed_weight, true);
         GL_LAUNCH_CHECK("teleport_count_kernel");
     }
     return GL_OK;

@@ -385,7 +385,7 @@ class FarFieldModel:
         in_deg = (indptr[1:] - indptr[:-1]).to(torch.float32)
         out_deg = torch.bincount(indices.to(torch.int64), minlength=n).to(torch.float32)
         f = torch.empty((n, FAR_F_IN), dtype=torch.float32, device=dev)
-        f[:, 0] = torch.log(n * st["pagerank"].clamp_min(0) + 1e-6) / 10.0
+        f[:, 0] = torch.log(n * ws.pagerank(alpha).clamp_min(0) + 1e-6) / 10.0
         f[:, 1] = torch.log(n * st["near_uniform"].clamp_min(0) + 1e-6) / 10.0
         f[:, 2] = torch.log(n * st["expected"].clamp_min(0) + 1e-6) / 10.0
         f[:, 3] = torch.log1p(in_deg)

@@ -16,9 +16,10 @@ inverses, ``csrc/window_start.cu``) plus the mass it misses, spread along a
 far-field shape:
 
 * ``"expected"`` (default): the far field of the uniform teleport vector,
-  i.e. the global PageRank vector minus its own near field, normalized.  For
-  seed sets drawn uniformly at random this is the expected far field of a
-  query (PPR is linear in v), computed once per graph and damping factor.
+  normalized — solved directly as the PPR vector whose teleport is where
+  the uniform vector's next window exits land.  For seed sets drawn
+  uniformly at random this is the expected far field of a query (PPR is
+  linear in v), computed once per graph and damping factor.
 * ``"pagerank"``: the global PageRank vector.
 * ``"learned"``: a per-node density predicted by the warm-start network
   (``warmstart.FarFieldModel``) from node features, trained on far fields of
@@ -152,26 +153,35 @@ class WindowStart:
         st = {"inv": inv, "alpha": float(alpha)}
         self._alpha[key] = st          # the far-field shapes below use the inverses
         try:
-            st["pagerank"] = self._pagerank(alpha)
-            torch.cuda.synchronize(self.dev)
-            t2 = time.perf_counter()
-            st["near_uniform"], st["expected"] = self._expected_far_field(alpha, st["pagerank"])
+            st["near_uniform"], st["expected"] = self._expected_far_field(alpha)
             st["shape"] = self._shape(st)
         except BaseException:
             del self._alpha[key]
             raise
         torch.cuda.synchronize(self.dev)
-        t3 = time.perf_counter()
-        self.setup_seconds[key] = t3 - t0
-        self.setup_phases[key] = {"inverses_s": round(t1 - t0, 4), "pagerank_s": round(t2 - t1, 4),
-                                  "far_field_s": round(t3 - t2, 4)}
+        t2 = time.perf_counter()
+        self.setup_seconds[key] = t2 - t0
+        self.setup_phases[key] = {"inverses_s": round(t1 - t0, 4), "far_field_s": round(t2 - t1, 4)}
         return st
+
+    def pagerank(self, alpha: float) -> torch.Tensor:
+        """Global PageRank (uniform teleport) of the engine's graph, FP32 [n]
+        (computed on first use: the ``pagerank`` shape and the learned model's
+        features need it, the default start does not)."""
+        st = self._prepare(alpha)
+        if "pagerank" not in st:
+            n = self.eng.n
+            res = self.eng.solve([np.arange(n)], alpha=alpha, tol=1e-6, max_iterations=1000, retire=False,
+                                 use_graphs=False)
+            x = res.X[:, 0].clamp_min(0)
+            st["pagerank"] = (x / x.sum()).contiguous()
+        return st["pagerank"]
 
     def _shape(self, st: dict) -> torch.Tensor:
         if self.shape_kind == "expected":
             return st["expected"]
         if self.shape_kind == "pagerank":
-            return st["pagerank"]
+            return self.pagerank(st["alpha"])
         return self.model.shape(self, st["alpha"])
 
     def set_shape(self, shape: str, far_field_model=None) -> None:
@@ -187,28 +197,38 @@ class WindowStart:
         for st in self._alpha.values():
             st["shape"] = self._shape(st)
 
-    def _pagerank(self, alpha: float) -> torch.Tensor:
-        """Global PageRank (uniform teleport) of the engine's graph, FP32 [n],
-        to a certified L1 distance of 1e-5: it only shapes the far field of a
-        start (an error there costs a start its accuracy, not the solve its
-        fixed point), and a tighter bound runs into the rounding floor of an
-        FP32 column of millions of entries."""
-        n = self.eng.n
-        res = self.eng.solve([np.arange(n)], alpha=alpha, tol=1e-5, max_iterations=300, retire=False,
-                             use_graphs=False)
-        x = res.X[:, 0].clamp_min(0)
-        return (x / x.sum()).contiguous()
+    def _expected_far_field(self, alpha: float):
+        """(near field of the uniform teleport vector u, u's far field
+        normalized).
 
-    def _expected_far_field(self, alpha: float, pagerank: torch.Tensor):
-        """(near field of the uniform teleport vector, its far field: PageRank
-        minus that near field, normalized; non-negative up to rounding)."""
-        n = self.eng.n
-        near = self.near_field([np.arange(n)], alpha)[:, 0].contiguous()
-        far = (pagerank - near).clamp_min(0)
-        tot = far.sum()
-        if not bool(tot > 0):
-            return near, pagerank
-        return near, (far / tot).contiguous()
+        The far field is the series' tail, (1 - alpha) sum_{k > L} y_k =
+        (1 - alpha) (I - alpha A)^-1 (alpha M y_L): the PPR vector whose
+        teleport is where the next window exits land, M y_L.  It is solved
+        as such (one column, no dangling term in the landing vector; the
+        graph's dangling mass returns through it as for any query) rather
+        than as PageRank minus the near field, whose difference is a small
+        fraction of either (about 1 % after 8 exits) and would carry their
+        rounding and truncation errors magnified by that factor."""
+        eng = self.eng
+        n = eng.n
+        _, tp, V = self._teleport([np.arange(n)])
+        near, _, y_last = self._near_field(V, tp, alpha, want_last=True)
+        land = torch.empty_like(y_last)
+        self.off.spmm(y_last, land)
+        land = land[:, 0].clamp_min(0)
+        tot = land.sum()
+        near = near[:, 0].contiguous()
+        if not bool(tot > 0):                   # nothing leaves the windows: any shape will do
+            return near, torch.full((n,), 1.0 / n, dtype=torch.float32, device=self.dev)
+        land = (land / tot).to(torch.float32)
+        rows = torch.nonzero(land > 0).flatten().to(torch.int32)
+        ptr = torch.tensor([0, rows.numel()], dtype=torch.int32, device=self.dev)
+        tpl = teleport_from_seed_sets(ptr, rows, n, eng.block_size, land[rows.long()].contiguous())
+        run = PprRun(eng.meta, n, n, eng.block_size, eng.block_size, tpl, alpha, 1000,
+                     1e-6 * (1.0 - alpha) / alpha, native.GL_PPR_STOP_ALL, eng.dbits)
+        res = run.run(chunk=8)
+        far = res.X[:, 0].clamp_min(0)
+        return near, (far / far.sum()).contiguous()
 
     # -- start vectors ------------------------------------------------------------
     def _teleport(self, seed_sets, tel: tuple | None = None):
@@ -219,7 +239,7 @@ class WindowStart:
         tp = teleport_from_seed_sets(ptr, rows, eng.n, eng.block_size, w)
         return tel, tp, eng.teleport_columns(seed_sets, tel)
 
-    def _near_field(self, V: torch.Tensor, tp, alpha: float):
+    def _near_field(self, V: torch.Tensor, tp, alpha: float, want_last: bool = False):
         """(near field [n, K], per-window column sums [windows, K]) of the
         teleport columns V.
 
@@ -240,7 +260,7 @@ class WindowStart:
         a = float(alpha)
         nf = torch.empty_like(V)
         partial = torch.empty((self.windows, K), dtype=torch.float32, device=self.dev)
-        Y = torch.empty_like(V) if self.leaves else None
+        Y = torch.empty_like(V) if (self.leaves or want_last) else None
         native.check(L.gl_window_apply(inv.data_ptr(), n, K, V.data_ptr(), 1.0,
                                        Y.data_ptr() if Y is not None else None, nf.data_ptr(), 1.0 - a, 1,
                                        partial.data_ptr(), s))
@@ -248,10 +268,12 @@ class WindowStart:
             T = torch.empty_like(V)
             for k in range(1, self.leaves + 1):
                 self.off.spmm(Y, T)
-                last = k == self.leaves
+                last = k == self.leaves and not want_last
                 native.check(L.gl_window_apply(inv.data_ptr(), n, K, T.data_ptr(), a,
                                                None if last else Y.data_ptr(), nf.data_ptr(), 1.0 - a, 0,
                                                partial.data_ptr(), s))
+        if want_last:
+            return nf, partial, Y
         return nf, partial
 
     def near_field(self, seed_sets, alpha: float) -> torch.Tensor:

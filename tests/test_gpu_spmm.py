@@ -209,3 +209,53 @@ def test_spmm_float64_heavy_stripes_one_column_tiles(F, device):
     pbr = _gl().csr_to_pbr(A, block_rows=8, block_cols=8, min_nnz_per_block=2).to(device)
     Y = _gl().pbr_matmul(pbr, torch.from_numpy(X).to(device)).cpu().numpy()
     assert np.allclose(Y, spmm_csr_fp64(A, X), rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.skipif(not torch.cuda.is_available() or torch.cuda.device_count() < 2,
+                    reason="needs two visible GPUs")
+def test_spmm_wide_tiles_on_a_second_device():
+    """The per-device launch attributes: a 128-column FP32 SpMM (dynamic
+    shared memory above the 48 KiB default) on device 1 after device 0."""
+    gl = _gl()
+    A = random_csr(2048, 0.01, seed=21)
+    X = random_x(2048, 128, seed=3)
+    Yref = spmm_csr_fp64(A, X)
+    for dev in ("cuda:0", "cuda:1"):
+        pbr = gl.csr_to_pbr(A, block_rows=8, block_cols=8, min_nnz_per_block=2).to(dev)
+        Y = gl.pbr_matmul(pbr, torch.from_numpy(X).to(dev)).cpu().numpy()
+        _check(Y, Yref)
+
+
+def test_spmm_from_two_host_threads(device):
+    """Two host threads launching wide SpMMs on their own streams at once
+    (the HTTP server's thread pool does this): both results exact."""
+    import threading
+    gl = _gl()
+    A = random_csr(4096, 0.004, seed=22)
+    X = random_x(4096, 128, seed=4)
+    Yref = spmm_csr_fp64(A, X)
+    pbr = gl.csr_to_pbr(A, block_rows=8, block_cols=8, min_nnz_per_block=2).to(device)
+    Xd = torch.from_numpy(X).to(device)
+    out, errors = {}, []
+
+    def work(k):
+        try:
+            idx = torch.device(device).index
+            torch.cuda.set_device(idx if idx is not None else torch.cuda.current_device())
+            s = torch.cuda.Stream(device)
+            with torch.cuda.stream(s):
+                ys = [gl.pbr_matmul(pbr, Xd) for _ in range(4)]
+            s.synchronize()
+            out[k] = [y.cpu().numpy() for y in ys]
+        except BaseException as exc:        # surfaced below
+            errors.append(exc)
+
+    ts = [threading.Thread(target=work, args=(k,)) for k in range(2)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join(120)
+    assert not errors, errors
+    for k in range(2):
+        for Y in out[k]:
+            _check(Y, Yref)
