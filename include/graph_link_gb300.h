@@ -397,6 +397,28 @@ int gl_ppr_step(const gl_pbr_matrix* A, const gl_teleport* tp,
  * that advances chunk_base at the end of a captured chunk of steps). */
 int gl_counter_add(int32_t* counter, int32_t delta, cudaStream_t stream);
 
+typedef struct gl_ppr_run_result {
+    int32_t iterations;    /* steps until the stop rule held (max_iterations if it never did) */
+    int32_t converged;     /* 1 when the stop rule held                                      */
+    int32_t result_in_x1;  /* 1: the final iterate is in X1; 0: in X0                         */
+} gl_ppr_run_result;
+
+/* The whole power iteration in one call (the loop of run_personalized_pagerank,
+ * graph_link/__init__.py:210-271, which reads the residual back after every
+ * step; here once per chunk of `chunk` steps): gl_ppr_step until the stop
+ * rule of params->stop_mode holds or params->max_iterations steps ran.
+ * params as for gl_ppr_step (step_in_chunk is set here; residual_hist,
+ * dangling_hist and *chunk_base are zeroed here).  X0 holds the start
+ * [rows][K] (init_from_teleport = 1: X0 is first set to the teleport
+ * vectors), X1 is the second iterate buffer; result->result_in_x1 says which
+ * holds the answer.  column_iterations (host, K entries, or NULL) receives
+ * each column's first step below its threshold (-1: none).  Synchronizes
+ * the stream once per chunk. */
+int gl_ppr_run(const gl_pbr_matrix* A, const gl_teleport* tp, void* X0, void* X1, int64_t K,
+               const gl_ppr_step_params* params, int32_t init_from_teleport, int32_t chunk,
+               void* workspace, int64_t workspace_bytes, int32_t* column_iterations,
+               gl_ppr_run_result* result, cudaStream_t stream);
+
 /* ======================================================================== */
 /* Top-k of PPR columns                                                     */
 /* The reference returns all N ranks and leaves the top-X cut to its        */

@@ -584,3 +584,87 @@ extern "C" int gl_counter_add(int32_t* counter, int32_t delta, cudaStream_t stre
     GL_LAUNCH_CHECK("counter_add_kernel");
     return GL_OK;
 }
+
+// The whole power iteration behind one call: chunks of `chunk` fused steps
+// (gl_ppr_step; step t reads buffer t % 2 and writes the other), one read of
+// the chunk's residual rows per chunk, the stop rule checked on the host.
+// Steps past the stop (STOP_ALL) or past max_iterations are no-ops on the
+// device, so a chunk is always launched whole.
+extern "C" int gl_ppr_run(const gl_pbr_matrix* A, const gl_teleport* tp, void* X0, void* X1, int64_t K,
+                          const gl_ppr_step_params* params, int32_t init_from_teleport, int32_t chunk,
+                          void* workspace, int64_t workspace_bytes, int32_t* column_iterations,
+                          gl_ppr_run_result* result, cudaStream_t stream) {
+    GL_REQUIRE(A && tp && X0 && X1 && params && result, GL_ERR_INVALID_ARGUMENT, "NULL argument");
+    GL_REQUIRE(X0 != X1, GL_ERR_INVALID_ARGUMENT, "X0 and X1 must be different buffers");
+    GL_REQUIRE(K >= 0 && K < (int64_t)INT32_MAX && chunk >= 1 && params->max_iterations >= 0,
+               GL_ERR_INVALID_ARGUMENT, "bad K / chunk / max_iterations");
+    gl_ppr_step_params p = *params;
+    GL_REQUIRE(p.chunk_base && p.residual_hist && p.dangling_hist, GL_ERR_INVALID_ARGUMENT,
+               "NULL iteration buffers");
+    const int32_t max_it = p.max_iterations;
+    const int64_t rows = A->rows;
+    result->iterations = max_it;
+    result->converged = 0;
+    result->result_in_x1 = 0;
+    GL_CUDA_TRY(cudaMemsetAsync(p.residual_hist, 0, sizeof(double) * (size_t)(max_it > 0 ? max_it : 1) * K, stream));
+    GL_CUDA_TRY(cudaMemsetAsync(p.dangling_hist, 0, sizeof(double) * (size_t)(max_it + 1) * K, stream));
+    GL_CUDA_TRY(cudaMemsetAsync(const_cast<int32_t*>(p.chunk_base), 0, sizeof(int32_t), stream));
+    int rc = GL_OK;
+    if (init_from_teleport)
+        rc = gl_ppr_init(tp, rows, K, A->value_type, X0, p.dangling_bitmap,
+                         p.dangling_bitmap ? p.dangling_hist : nullptr, stream);
+    else if (p.dangling_bitmap)
+        rc = gl_ppr_dangling_mass(X0, rows, K, A->value_type, p.dangling_bitmap, p.dangling_hist, stream);
+    if (rc != GL_OK) return rc;
+    std::vector<double> thr((size_t)K, p.tol);
+    if (p.stop_mode == GL_PPR_STOP_PER_COLUMN && p.column_tol && K > 0)
+        GL_CUDA_TRY(cudaMemcpyAsync(thr.data(), p.column_tol, sizeof(double) * K, cudaMemcpyDeviceToHost, stream));
+    std::vector<double> res((size_t)chunk * (size_t)K);
+    std::vector<int32_t> first((size_t)K, -1);
+    void* bufs[2] = {X0, X1};
+    int64_t done = 0, written = max_it;
+    int64_t finished = 0;
+    bool stop = K == 0 || rows == 0;
+    if (stop) {
+        result->iterations = 0;
+        result->converged = 1;
+        written = 0;
+    }
+    while (!stop && done < max_it) {
+        for (int32_t i = 0; i < chunk; ++i) {
+            p.step_in_chunk = i;
+            rc = gl_ppr_step(A, tp, bufs[(done + i) & 1], bufs[(done + i + 1) & 1], K, &p, workspace,
+                             workspace_bytes, stream);
+            if (rc != GL_OK) return rc;
+        }
+        rc = gl_counter_add(const_cast<int32_t*>(p.chunk_base), chunk, stream);
+        if (rc != GL_OK) return rc;
+        const int64_t n = std::min<int64_t>(chunk, max_it - done);
+        GL_CUDA_TRY(cudaMemcpyAsync(res.data(), p.residual_hist + done * K, sizeof(double) * (size_t)(n * K),
+                                    cudaMemcpyDeviceToHost, stream));
+        GL_CUDA_TRY(cudaStreamSynchronize(stream));
+        for (int64_t t = 0; t < n && !stop; ++t) {
+            const double* row = res.data() + t * K;
+            double worst = 0.0;
+            for (int64_t k = 0; k < K; ++k) {
+                worst = std::max(worst, row[k]);
+                if (first[k] < 0 && row[k] < thr[k]) {
+                    first[k] = (int32_t)(done + t + 1);
+                    ++finished;
+                }
+            }
+            if (p.stop_mode == GL_PPR_STOP_ALL ? worst < p.tol : finished == K) {
+                result->iterations = (int32_t)(done + t + 1);
+                result->converged = 1;
+                // STOP_ALL: the steps after the stop wrote nothing; per column,
+                // stopped columns are carried into every later buffer
+                written = p.stop_mode == GL_PPR_STOP_ALL ? done + t + 1 : std::min<int64_t>(done + chunk, max_it);
+                stop = true;
+            }
+        }
+        done += chunk;
+    }
+    result->result_in_x1 = (int32_t)(written & 1);
+    if (column_iterations && K > 0) std::copy(first.begin(), first.end(), column_iterations);
+    return GL_OK;
+}

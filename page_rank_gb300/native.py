@@ -148,6 +148,10 @@ class PprStepParams(_c.Structure):
                 ("dangling_target", _i32), ("column_alpha", _vp), ("column_tol", _vp)]
 
 
+class PprRunResult(_c.Structure):
+    _fields_ = [("iterations", _i32), ("converged", _i32), ("result_in_x1", _i32)]
+
+
 # name -> (restype, argtypes)
 _SIGS = {
     "gl_last_error": (_c.c_char_p, []),
@@ -180,6 +184,9 @@ _SIGS = {
     "gl_ppr_step": (_c.c_int, [_c.POINTER(PbrMatrixDesc), _c.POINTER(TeleportDesc), _vp, _vp, _i64,
                                _c.POINTER(PprStepParams), _vp, _i64, _vp]),
     "gl_counter_add": (_c.c_int, [_vp, _i32, _vp]),
+    "gl_ppr_run": (_c.c_int, [_c.POINTER(PbrMatrixDesc), _c.POINTER(TeleportDesc), _vp, _vp, _i64,
+                              _c.POINTER(PprStepParams), _i32, _i32, _vp, _i64, _vp,
+                              _c.POINTER(PprRunResult), _vp]),
     "gl_topk_workspace_bytes": (_i64, [_i64, _i64, _i32]),
     "gl_topk_columns": (_c.c_int, [_vp, _i64, _i64, _vp, _i64, _i32, _vp, _vp, _vp, _i64, _vp]),
     "gl_mlp_forward": (_c.c_int, [_vp, _i64, _i32, _vp, _vp, _vp, _c.c_float, _vp, _vp]),

@@ -212,6 +212,22 @@ class PprRun:
                                            self._step_params(i), self.ws.data_ptr(), self._ws_bytes, st))
             native.check(L.gl_counter_add(self.chunk_base.data_ptr(), n, st))
 
+    def run_native(self, chunk: int = 8, x0: torch.Tensor | None = None) -> PprResult:
+        """The same run with the loop inside the library (``gl_ppr_run``):
+        chunks of fused steps, one residual read per chunk."""
+        chunk = max(2, chunk + (chunk % 2))
+        if x0 is not None:
+            self.bufs[0].copy_(x0)
+        p = self._step_params(0)
+        out = native.PprRunResult()
+        col_it = np.full(self.K, -1, dtype=np.int32)
+        native.check(native.lib().gl_ppr_run(
+            self._desc, self._tpd, self.bufs[0].data_ptr(), self.bufs[1].data_ptr(), self.K, p,
+            1 if x0 is None else 0, chunk, self.ws.data_ptr(), self._ws_bytes,
+            col_it.ctypes.data if self.K else None, out, self._stream()))
+        return PprResult(X=self.bufs[out.result_in_x1], iterations=int(out.iterations),
+                         converged=bool(out.converged), column_iterations=col_it.astype(np.int64))
+
     def capture(self, chunk: int):
         """CUDA graph of one chunk of steps over this run's buffers (the steps
         read their iteration number from the device counter, so one graph

@@ -135,3 +135,34 @@ def test_ppr_per_column_alpha_matches_scalar_runs(K, device):
         want, _, ok, _ = oppr.power_iteration_fp64(g.A, V[:, cols], a, 5000, 1e-14, g.dangling)
         assert ok
         assert np.abs(X[:, cols] - want).sum(axis=0).max() <= 1e-6
+
+
+@pytest.mark.parametrize("stop_mode", ["all", "per_column"])
+@pytest.mark.parametrize("warm", [False, True])
+def test_library_run_loop_matches_the_host_loop(stop_mode, warm, device):
+    """gl_ppr_run (the loop inside the library) against PprRun.run (the host
+    loop over gl_ppr_step): same iterations, same vectors bit for bit."""
+    from page_rank_gb300 import native, synth
+    from page_rank_gb300.graph_link.pbr_registry import get_pbr_gpu_meta
+    from page_rank_gb300.ppr import PprRun, dangling_bitmap, teleport_from_seed_sets
+    g = synth.cluster_zipf_graph(log2n=13, mean_degree=12.0, seed=4)
+    from page_rank_gb300 import graph_link as gl
+    pbr = gl.csr_to_pbr(g.A, block_rows=4, block_cols=4, min_nnz_per_block=4).to(device)
+    meta = get_pbr_gpu_meta(pbr)
+    sets = synth.seed_sets(g.n, 11, 1, 9, seed=5)
+    ptr = torch.tensor(np.concatenate([[0], np.cumsum([len(s) for s in sets])]), dtype=torch.int32, device=device)
+    idx = torch.tensor(np.concatenate(sets), dtype=torch.int32, device=device)
+    tp = teleport_from_seed_sets(ptr, idx, g.n, 4)
+    dbits = dangling_bitmap(torch.from_numpy(g.A.indices.astype(np.int32)).to(device), g.n)
+    mode = native.GL_PPR_STOP_ALL if stop_mode == "all" else native.GL_PPR_STOP_PER_COLUMN
+    x0 = None
+    if warm:
+        x0 = torch.rand((g.n, len(sets)), device=device, generator=torch.Generator(device=device).manual_seed(1))
+        x0 /= x0.sum(dim=0, keepdim=True)
+    runs = [PprRun(meta, g.n, g.n, 4, 4, tp, 0.85, 300, 1e-7, mode, dbits) for _ in range(2)]
+    a = runs[0].run(chunk=8, x0=x0)
+    b = runs[1].run_native(chunk=8, x0=x0)
+    assert a.converged and b.converged and a.iterations == b.iterations
+    assert torch.equal(a.X, b.X)
+    if mode == native.GL_PPR_STOP_PER_COLUMN:
+        assert np.array_equal(a.column_iterations, b.column_iterations)
