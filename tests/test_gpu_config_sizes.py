@@ -93,17 +93,20 @@ def test_batched_ppr_configuration_sampled_columns(device):
 
 
 def test_warm_start_configuration_warm_and_cold_against_fp64(device):
+    """The window-solve start (the product's warm start) and the cold start
+    on the 2^21-node configuration: both within the certified L1 of the FP64
+    fixed point, the start with at least 1.5x fewer power iterations."""
     from page_rank_gb300 import synth
     from page_rank_gb300.engine import PPREngine
-    from page_rank_gb300.warmstart import WarmStart
+    from page_rank_gb300.window_start import WindowStart
     g = synth.cluster_zipf_graph(log2n=21, mean_degree=20.0, seed=3, device=device)
-    eng = PPREngine(g.A, block_size=8, min_nnz_per_block=4, device=device, dangling=g.dangling)
-    ws = WarmStart(eng, seed=0)
-    ws.train(num_vectors=512, batch=256, nodes_per_vector=512, epochs=2)
+    eng = PPREngine(g.A, block_size=4, min_nnz_per_block=4, device=device, dangling=g.dangling)
+    ws = WindowStart(eng)
     sets = synth.seed_sets(g.n, 8, 1, 32, seed=424242)
     cold = eng.solve(sets, tol=L1_TOL)
     warm = ws.solve(sets, tol=L1_TOL)
-    assert cold.converged.all() and warm.converged.all()
+    assert cold.converged.all() and warm.converged.all() and warm.warm_columns.all()
+    assert cold.iterations.mean() >= 1.5 * warm.iterations.mean()
     for res in (cold, warm):
         d = _fp64_distance(g.A, g.dangling, res.X.double().cpu().numpy(), sets, [0.85] * len(sets))
         assert (d <= L1_TOL).all(), d
@@ -111,21 +114,15 @@ def test_warm_start_configuration_warm_and_cold_against_fp64(device):
 
 def test_serving_configuration_sampled_requests_against_fp64(device):
     from page_rank_gb300 import synth
-    from page_rank_gb300.engine import PPREngine
     from page_rank_gb300.serving import PPRServer
-    from page_rank_gb300.warmstart import WarmStart
-    gt = synth.cluster_zipf_graph(log2n=16, mean_degree=20.0, seed=99)
-    model = WarmStart(PPREngine(gt.A, block_size=8, min_nnz_per_block=4, device=device, dangling=gt.dangling),
-                      seed=0)
-    model.train(num_vectors=512, batch=256, nodes_per_vector=512, epochs=2)
+    from page_rank_gb300.warmstart import WarmStartGate
+    from page_rank_gb300.window_start import WindowStart
     graphs = {f"g{i}": synth.cluster_zipf_graph(log2n=lg, mean_degree=20.0, seed=200 + i, device=device)
               for i, lg in enumerate((16, 18, 20))}
     srv = PPRServer(device=device, chunk=8)
     for name, g in graphs.items():
         eng = srv.add_graph(name, g.A, dangling=g.dangling, block_size=8, min_nnz=4)
-        w = WarmStart(eng, seed=0)
-        w.mlp = model.mlp
-        srv.warm[name] = w
+        srv.warm[name] = WindowStart(eng, gate=WarmStartGate())
     rng = np.random.default_rng(7)
     reqs = []
     for wave in range(4):                     # requests arrive while others are on the GPU
