@@ -221,3 +221,42 @@ def test_run_personalized_pagerank_warm_start_argument(device):
     assert (Xc.double() - Xw.double()).abs().sum(dim=0).max().item() < 2e-6
     with pytest.raises(ValueError):
         gl.run_personalized_pagerank(pbr, src, warm_start=x0[:, :2])
+
+
+def test_ragged_graph_with_dangling_nodes(device):
+    """n not a multiple of the window (a short last window), dangling nodes
+    (their mass returns through each query's teleport vector in the solve;
+    the start ignores it), a seed set inside the short window: start vectors
+    against the oracle, the warm solve against the FP64 fixed point."""
+    from page_rank_gb300.engine import PPREngine
+    from page_rank_gb300.window_start import WindowStart
+    n = 1000
+    rng = np.random.default_rng(12)
+    rows, cols = [], []
+    for j in range(n):
+        if j % 17 == 0:
+            continue                                   # dangling
+        deg = int(rng.integers(1, 9))
+        loc = (j // 64) * 64 + rng.integers(0, 64, deg)        # mostly inside the window
+        far = rng.integers(0, n, 2)
+        for i in np.concatenate([loc, far]):
+            if i < n:
+                rows.append(i)
+                cols.append(j)
+    A = sp.csr_matrix((np.ones(len(rows)), (rows, cols)), shape=(n, n))
+    A.sum_duplicates()
+    colsum = np.asarray(A.sum(axis=0)).ravel()
+    A = sp.csr_matrix(A @ sp.diags(np.where(colsum > 0, 1.0 / np.maximum(colsum, 1), 0.0)), dtype=np.float32)
+    dangling = colsum == 0
+    eng = PPREngine(A, block_size=4, device=device, dangling=dangling)
+    ws = WindowStart(eng, leaves=3)
+    sets = [np.array([990, 999]), np.array([5]), np.arange(0, 1000, 97)]
+    x0 = ws.start(sets, 0.85).cpu().numpy().astype(np.float64)
+    far = ws._prepare(0.85)["shape"].cpu().numpy().astype(np.float64)
+    V = oppr.teleport_matrix(n, sets)
+    ref = ows.window_start(A, V, 0.85, 3, far)
+    assert np.abs(x0 - ref).sum(axis=0).max() <= 1e-5
+    warm = ws.solve(sets, alpha=0.85, tol=1e-6)
+    exact = oppr.direct_solve_fp64(A, V, 0.85, dangling)
+    assert warm.converged.all()
+    assert np.abs(warm.X.cpu().numpy().astype(np.float64) - exact).sum(axis=0).max() <= 1e-6
