@@ -833,6 +833,25 @@ stripe_kernel(const StripeArgs<S> a) {
             __syncthreads();
             if (s_skip) return;
         }
+        // STOP_PER_COLUMN: when every column stopped at step t - 1 or before
+        // (residuals of steps t - 2 and t - 1 below its threshold), the step
+        // that stopped it has already copied it into the other buffer, both
+        // buffers hold every final value, and this launch has nothing to do.
+        if (a.stop_mode == GL_PPR_STOP_PER_COLUMN && t >= 2) {
+            if (threadIdx.x < 32) {
+                bool all = true;
+                const double* p1 = a.res_hist + (int64_t)(t - 1) * a.K;
+                const double* p2 = a.res_hist + (int64_t)(t - 2) * a.K;
+                for (int k = lane; k < a.K; k += 32) {
+                    const double tl = a.col_tol ? a.col_tol[k] : a.tol;
+                    all = all && p1[k] < tl && p2[k] < tl;
+                }
+                const bool skip = __all_sync(0xffffffffu, all);
+                if (lane == 0) s_skip = skip ? 1 : 0;
+            }
+            __syncthreads();
+            if (s_skip) return;
+        }
     }
 
     // per-CTA column sums (residual, dangling) in shared memory behind the

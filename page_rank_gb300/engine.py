@@ -108,28 +108,14 @@ class PPREngine:
 
     # -- queries --------------------------------------------------------------
     def teleport(self, seed_sets) -> tuple:
-        ptr = np.zeros(len(seed_sets) + 1, dtype=np.int32)
-        ptr[1:] = np.cumsum([len(s) for s in seed_sets])
-        idx = np.concatenate([np.asarray(s, dtype=np.int32) for s in seed_sets]) if seed_sets else \
-            np.zeros(0, np.int32)
-        # duplicate seeds inside one set merge into one weighted entry so the
-        # kernel's epilogue sees unique (row, column) pairs
-        rows, cols, w = [], [], []
-        for k, s in enumerate(seed_sets):
-            u, c = np.unique(np.asarray(s, dtype=np.int64), return_counts=True)
-            rows.append(u)
-            cols.append(np.full(len(u), k))
-            w.append(c / c.sum())
-        if seed_sets:
-            rows = np.concatenate(rows).astype(np.int32)
-            w = np.concatenate(w).astype(np.float32)
-            ptr2 = np.zeros(len(seed_sets) + 1, dtype=np.int32)
-            ptr2[1:] = np.cumsum([len(np.unique(np.asarray(s))) for s in seed_sets])
-        else:
-            rows, w, ptr2 = idx, np.zeros(0, np.float32), ptr
+        """(seed_ptr [K+1], unique seed rows, weights) on the device: column k
+        teleports to the distinct seeds of set k, each weighted by its
+        multiplicity over the set's size (duplicates inside a set merge into
+        one weighted entry, so the step's epilogue sees unique (row, column)
+        pairs)."""
+        ptr, rows, w = seed_set_index(seed_sets)
         dev = self.device
-        return (torch.from_numpy(ptr2).to(dev), torch.from_numpy(rows).to(dev),
-                torch.from_numpy(w).to(dev))
+        return (torch.from_numpy(ptr).to(dev), torch.from_numpy(rows).to(dev), torch.from_numpy(w).to(dev))
 
     def teleport_columns(self, seed_sets, tel: tuple | None = None) -> torch.Tensor:
         """Dense teleport (personalization) vectors [n, K] of the seed sets
@@ -163,15 +149,17 @@ class PPREngine:
         t0 = time.perf_counter()   # the solve's time includes the warm start's prediction
         warm_columns = None
         pre_steps = 0
+        x0_owned = False                # x0 is ours to overwrite (not the caller's)
         if warm_start is not None and x0 is None:
             x0, warm_columns = warm_start.start_vectors(seed_sets, alpha)
             # steps the start already took from its vector (they count as
             # iterations of the columns that kept it)
             pre_steps = int(getattr(warm_start, "pre_steps", 0))
+            x0_owned = True
         thr = certified_tolerance(tol, alpha) if certified else tol
         with torch.cuda.device(dev):
             ptr, rows, w = self.teleport(seed_sets)
-            out = torch.empty((self.n, K), dtype=torch.float32, device=dev)
+            out = None                  # allocated when a run ends with columns still going
             col_iter = np.full(K, -1, dtype=np.int64)
             active = np.arange(K)
             cur_x0 = x0
@@ -186,14 +174,17 @@ class PPREngine:
                              max_iterations - done, thr,
                              native.GL_PPR_STOP_PER_COLUMN if retire else native.GL_PPR_STOP_ALL,
                              self.dbits)
-                run.init(cur_x0)
+                run.init(cur_x0, adopt=x0_owned or cur_x0 is not x0)
                 graph = None
                 steps = 0            # steps launched in this run
                 written = 0          # steps that wrote a new iterate
                 stop_all_at = None
                 fin = np.zeros(active.size, dtype=bool)
                 while steps < run.max_iterations:
-                    if use_graphs:
+                    # a run's first chunk is launched directly: warm-started
+                    # and nearly finished runs often end inside it, where a
+                    # captured graph would not repay its capture
+                    if use_graphs and steps > 0:
                         if graph is None:
                             graph = self._capture(run, chunk)
                         graph.replay()
@@ -226,13 +217,19 @@ class PPREngine:
                 else:
                     keep_out = ~keep
                 sel = np.nonzero(keep_out)[0]
-                if sel.size:
+                if sel.size == K and out is None:
+                    out = Xcur          # the whole batch ended in this run, in column order
+                elif sel.size:
+                    if out is None:
+                        out = torch.empty((self.n, K), dtype=torch.float32, device=dev)
                     out[:, torch.from_numpy(active[sel]).to(dev)] = Xcur[:, torch.from_numpy(sel).to(dev)]
                 if retire and keep.any() and done < max_iterations:
                     cur_x0 = Xcur[:, torch.from_numpy(np.nonzero(keep)[0]).to(dev)].contiguous()
                     active = active[keep]
                 else:
                     active = active[:0]
+            if out is None:             # max_iterations = 0
+                out = torch.empty((self.n, K), dtype=torch.float32, device=dev)
             torch.cuda.synchronize(dev)
         if isinstance(warm_columns, torch.Tensor):
             warm_columns = warm_columns.cpu().numpy()
@@ -269,6 +266,28 @@ class PPREngine:
     def _capture(self, run: PprRun, chunk: int):
         """CUDA graph of one chunk of steps for this run's buffers."""
         return run.capture(chunk)
+
+
+def seed_set_index(seed_sets) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Host CSR of seed sets: (ptr int32 [K+1], distinct rows per set in
+    increasing order int32, weight float32 = multiplicity / set size)."""
+    K = len(seed_sets)
+    lens = np.fromiter((len(s) for s in seed_sets), count=K, dtype=np.int64)
+    if K == 0 or lens.sum() == 0:
+        return np.zeros(K + 1, np.int32), np.zeros(0, np.int32), np.zeros(0, np.float32)
+    cols = np.repeat(np.arange(K, dtype=np.int64), lens)
+    idx = np.concatenate([np.asarray(s, dtype=np.int64).ravel() for s in seed_sets])
+    order = np.lexsort((idx, cols))
+    c, r = cols[order], idx[order]
+    head = np.ones(r.size, dtype=bool)
+    head[1:] = (c[1:] != c[:-1]) | (r[1:] != r[:-1])
+    starts = np.flatnonzero(head)
+    mult = np.diff(np.append(starts, r.size))
+    uc, ur = c[starts], r[starts]
+    ptr = np.zeros(K + 1, dtype=np.int32)
+    ptr[1:] = np.cumsum(np.bincount(uc, minlength=K))
+    w = (mult / lens[uc]).astype(np.float32)
+    return ptr, ur.astype(np.int32), w
 
 
 def _select_columns(ptr: torch.Tensor, rows: torch.Tensor, w: torch.Tensor, active: np.ndarray):

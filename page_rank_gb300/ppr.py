@@ -152,7 +152,10 @@ class PprRun:
     def _stream(self) -> int:
         return torch.cuda.current_stream(self.device).cuda_stream
 
-    def init(self, x0: torch.Tensor | None = None) -> None:
+    def init(self, x0: torch.Tensor | None = None, adopt: bool = False) -> None:
+        """Start from the teleport vectors, or from x0 (copied; with ``adopt``
+        a contiguous x0 of the right shape and type becomes the first
+        iterate buffer itself and is overwritten by the run)."""
         L = native.lib()
         st = self._stream()
         dbits = _ptr(self.dangling_bits)
@@ -161,7 +164,11 @@ class PprRun:
                                        self.bufs[0].data_ptr(), dbits,
                                        self.dang_hist[0].data_ptr() if dbits else None, st))
         else:
-            self.bufs[0].copy_(x0)
+            if (adopt and x0.is_contiguous() and x0.shape == self.bufs[0].shape and x0.dtype == self.bufs[0].dtype
+                    and x0.device == self.bufs[0].device and x0.data_ptr() != self.bufs[1].data_ptr()):
+                self.bufs[0] = x0
+            else:
+                self.bufs[0].copy_(x0)
             if dbits:
                 native.check(L.gl_ppr_dangling_mass(self.bufs[0].data_ptr(), self.rows, self.K,
                                                     self._vtype, dbits, self.dang_hist[0].data_ptr(),

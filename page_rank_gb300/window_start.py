@@ -358,7 +358,7 @@ class WindowStart:
             return x0, np.ones(k, dtype=bool)
         run = PprRun(eng.meta, eng.n, eng.n, eng.block_size, eng.block_size, tp, alpha, 1, 0.0,
                      native.GL_PPR_STOP_ALL, eng.dbits)
-        run.init(x0)
+        run.init(x0, adopt=True)
         del x0
         run.launch_chunk(1)
         if ev is not None:
@@ -367,7 +367,8 @@ class WindowStart:
         r_cold = self._cold_residuals_device(seed_sets, alpha, tel)
         use = r_warm <= r_cold
         self.pre_steps = 1
-        X = torch.where(use[None, :], run.bufs[1], V)
+        X = run.bufs[1]
+        torch.where(use[None, :], X, V, out=X)      # the teleport vector where the start lost
         if ev is not None:
             host = torch.empty((2, k), dtype=torch.float64, pin_memory=True)
             host[0].copy_(r_warm, non_blocking=True)

@@ -142,3 +142,20 @@ def test_cpulist_parsing():
     assert _parse_cpulist("0-3,8,10-11\n") == [0, 1, 2, 3, 8, 10, 11]
     assert _parse_cpulist("") == []
     restore_cpus({"bound": False})          # nothing recorded: no change
+
+
+def test_seed_set_index_matches_per_set_unique():
+    """The engine's host seed-set index: distinct seeds per set in increasing
+    order, weight = multiplicity / set size (duplicates merge)."""
+    import numpy as np
+    from page_rank_gb300.engine import seed_set_index
+    rng = np.random.default_rng(3)
+    sets = [rng.integers(0, 50, rng.integers(1, 30)) for _ in range(100)] + [np.array([7, 7, 7]), np.arange(5)]
+    ptr, rows, w = seed_set_index(sets)
+    assert ptr.dtype == np.int32 and rows.dtype == np.int32 and w.dtype == np.float32
+    for k, s in enumerate(sets):
+        u, c = np.unique(s, return_counts=True)
+        assert np.array_equal(rows[ptr[k]:ptr[k + 1]], u)
+        assert np.allclose(w[ptr[k]:ptr[k + 1]], c / c.sum())
+    e_ptr, e_rows, e_w = seed_set_index([])
+    assert e_ptr.tolist() == [0] and e_rows.size == 0 and e_w.size == 0
