@@ -41,6 +41,13 @@ extern "C" {
 const char* gl_last_error(void);
 /* ABI version of this library (major * 100 + minor). */
 int gl_version(void);
+/* sizeof(gl_pbr_matrix) in this library: a binding that declares the
+ * descriptor itself (ctypes, cgo, JNI) checks its own size against it. */
+int64_t gl_pbr_matrix_bytes(void);
+/* sizeof of any struct this header declares, by name ("gl_pbr_matrix",
+ * "gl_pbr_build_counts", "gl_teleport", "gl_ppr_step_params",
+ * "gl_ppr_run_result"); -1 for another name. */
+int64_t gl_struct_bytes(const char* name);
 
 /*
  * A PBR matrix resident in device memory.  Field meaning follows the

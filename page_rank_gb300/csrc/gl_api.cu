@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
+#include <string>
 #include <vector>
 
 #include "gl_common.cuh"
@@ -284,6 +285,19 @@ using namespace gl;
 
 extern "C" const char* gl_last_error(void) { return last_error(); }
 extern "C" int gl_version(void) { return 102; }
+
+extern "C" int64_t gl_pbr_matrix_bytes(void) { return (int64_t)sizeof(gl_pbr_matrix); }
+
+extern "C" int64_t gl_struct_bytes(const char* name) {
+    if (name == nullptr) return -1;
+    const std::string n(name);
+    if (n == "gl_pbr_matrix") return (int64_t)sizeof(gl_pbr_matrix);
+    if (n == "gl_pbr_build_counts") return (int64_t)sizeof(gl_pbr_build_counts);
+    if (n == "gl_teleport") return (int64_t)sizeof(gl_teleport);
+    if (n == "gl_ppr_step_params") return (int64_t)sizeof(gl_ppr_step_params);
+    if (n == "gl_ppr_run_result") return (int64_t)sizeof(gl_ppr_run_result);
+    return -1;
+}
 
 extern "C" int64_t gl_pbr_spmm_workspace_bytes(const gl_pbr_matrix* A, int64_t batch, int64_t features) {
     if (A == nullptr || batch < 0 || features < 0) return -1;

@@ -156,6 +156,8 @@ class PprRunResult(_c.Structure):
 _SIGS = {
     "gl_last_error": (_c.c_char_p, []),
     "gl_version": (_c.c_int, []),
+    "gl_pbr_matrix_bytes": (_i64, []),
+    "gl_struct_bytes": (_i64, [_c.c_char_p]),
     "gl_edges_workspace_bytes": (_i64, [_i64, _i64]),
     "gl_edges_to_transition": (_c.c_int, [_i64, _i64, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _i64,
                                           _vp]),

@@ -19,7 +19,8 @@ class _Pbr(ctypes.Structure):
                                   "stripe_block_ptr")] + \
                [(n, _I32) for n in ("num_heavy", "num_pieces", "piece_work", "column_tile",
                                     "lane_split")] + \
-               [(n, _P) for n in ("heavy_of", "heavy_stripe", "heavy_first", "piece_heavy")]
+               [(n, _P) for n in ("heavy_of", "heavy_stripe", "heavy_first", "piece_heavy")] + \
+               [("kernel", _I32), ("piece_range", _P)]     # gl_pbr_matrix as of ABI 101 (gl_version())
 
 _lib.gl_pbr_stripe_index.argtypes = [_P, _I64, _I64, _I32, _P, _P, _P]
 _lib.gl_pbr_validate.argtypes = [ctypes.POINTER(_Pbr), _P, _P]
@@ -28,6 +29,10 @@ _lib.gl_pbr_schedule_elems.restype = _I64
 _lib.gl_pbr_schedule_build.argtypes = [ctypes.POINTER(_Pbr), _I32, _P, _I64, _P]
 _lib.gl_pbr_spmm_static.argtypes = [ctypes.POINTER(_Pbr), _P, _P, _I64, _I64, _P]
 _lib.gl_last_error.restype = ctypes.c_char_p
+_lib.gl_pbr_matrix_bytes.restype = _I64
+if _lib.gl_pbr_matrix_bytes() != ctypes.sizeof(_Pbr):      # a descriptor of another ABI version
+    raise ImportError(f"gl_pbr_matrix is {_lib.gl_pbr_matrix_bytes()} bytes in the library, "
+                      f"{ctypes.sizeof(_Pbr)} here")
 
 def _check(rc):
     if rc == 2: raise ValueError(_lib.gl_last_error().decode())     # reference's message

@@ -85,3 +85,30 @@ def test_argument_errors_need_no_gpu():
     assert lib.gl_topk_columns(None, 10, 4, None, 4, native.GL_TOPK_MAX + 1, None, None, None, 0,
                                None) == native.GL_ERR_INVALID_ARGUMENT
     assert lib.gl_topk_columns(None, 10, 4, None, 0, 5, None, None, None, 0, None) == native.GL_OK
+
+
+def test_descriptor_size_matches_the_library():
+    """The ctypes descriptors here and in the reference-side binding stub
+    have the library's sizeof(gl_pbr_matrix)."""
+    import ctypes
+    import importlib.util
+    import pathlib
+    lib = native.lib()
+    assert lib.gl_pbr_matrix_bytes() == ctypes.sizeof(native.PbrMatrixDesc)
+    stub = pathlib.Path(__file__).with_name("ref_binding_stub.py").read_text()
+    ns: dict = {}
+    src = stub.split("_lib = ctypes.CDLL")[0] + "\n_P, _I32, _I64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64\n"
+    cls = stub[stub.index("class _Pbr"):stub.index("_lib.gl_pbr_stripe_index")]
+    exec(src + cls, ns)
+    assert ctypes.sizeof(ns["_Pbr"]) == lib.gl_pbr_matrix_bytes()
+
+
+def test_every_ctypes_struct_matches_the_library():
+    import ctypes
+    lib = native.lib()
+    pairs = {"gl_pbr_matrix": native.PbrMatrixDesc, "gl_pbr_build_counts": native.BuildCounts,
+             "gl_teleport": native.TeleportDesc, "gl_ppr_step_params": native.PprStepParams,
+             "gl_ppr_run_result": native.PprRunResult}
+    for name, cls in pairs.items():
+        assert lib.gl_struct_bytes(name.encode()) == ctypes.sizeof(cls), name
+    assert lib.gl_struct_bytes(b"no_such_struct") == -1
