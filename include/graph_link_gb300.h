@@ -518,8 +518,10 @@ int gl_window_finalize(float* near_field, int64_t n, int32_t K, const float* par
  * out[c] = || P(v_c) - v_c ||_1 for P(x) = alpha A x + ((1 - alpha) +
  * alpha d(x)) v_c, d(x) the mass on dangling nodes (bitmap, may be NULL).
  * colsum[j] = sum_i A[i][j] (FP64).  The seed sets are the teleport index
- * (seed_ptr [K + 1], unique seed_rows, seed_weights); A's column indices
- * must be sorted within each row.  A seed outside [0, n) gives -1. */
+ * (seed_ptr [K + 1], seed_rows unique and increasing within each column,
+ * seed_weights); A's column indices must be sorted within each row.  Work
+ * per column is bounded by the entries of its seed rows.  A seed outside
+ * [0, n) gives -1. */
 int gl_cold_residual(const int32_t* indptr, const int32_t* indices, const float* data, const double* colsum,
                      const uint32_t* dangling_bits, int64_t n, const int32_t* seed_ptr, const int32_t* seed_rows,
                      const float* seed_weights, int32_t K, float alpha, double* out, cudaStream_t stream);

@@ -386,21 +386,42 @@ __global__ void cold_residual_kernel(const int32_t* __restrict__ indptr, const i
             dmass += __shfl_xor_sync(0xffffffffu, dmass, o);
             bad += __shfl_xor_sync(0xffffffffu, bad, o);
         }
-        // (A v)_i for each seed row i: lanes over the seed rows, each looks up every seed column
+        // (A v)_i for each seed row i, lanes over the seed rows.  Per row the
+        // cheaper of two lookups: walk the row and binary-search each entry
+        // in the (sorted) seed list, or binary-search each seed in the row
+        // (sorted columns); so a column's cost is bounded by the entries of
+        // its seed rows, also for a seed set of millions of nodes.
         double in_seed = 0.0, corr = 0.0;
         if (bad == 0.0) {
+            int lg_m = 1;
+            while ((1 << lg_m) < m) ++lg_m;
             for (int k = lane; k < m; k += 32) {
                 const int32_t i = srows[s0 + k];
                 const int32_t r0 = indptr[i], r1 = indptr[i + 1];
+                const int32_t deg = r1 - r0;
+                int lg_d = 1;
+                while ((1 << lg_d) < deg) ++lg_d;
                 double av = 0.0;
-                for (int q = 0; q < m; ++q) {
-                    const int32_t s = srows[s0 + q];
-                    int32_t lo = r0, hi = r1;        // first entry with column >= s
-                    while (lo < hi) {
-                        const int32_t mid = lo + ((hi - lo) >> 1);
-                        if (indices[mid] < s) lo = mid + 1; else hi = mid;
+                if ((int64_t)deg * lg_m <= (int64_t)m * lg_d) {
+                    for (int32_t j = r0; j < r1; ++j) {
+                        const int32_t c = indices[j];
+                        int32_t lo = s0, hi = s1;            // c in the seed list?
+                        while (lo < hi) {
+                            const int32_t mid = lo + ((hi - lo) >> 1);
+                            if (srows[mid] < c) lo = mid + 1; else hi = mid;
+                        }
+                        if (lo < s1 && srows[lo] == c) av += (double)data[j] * sw[lo];
                     }
-                    for (int32_t j = lo; j < r1 && indices[j] == s; ++j) av += (double)data[j] * sw[s0 + q];
+                } else {
+                    for (int q = 0; q < m; ++q) {
+                        const int32_t sq = srows[s0 + q];
+                        int32_t lo = r0, hi = r1;            // first entry with column >= sq
+                        while (lo < hi) {
+                            const int32_t mid = lo + ((hi - lo) >> 1);
+                            if (indices[mid] < sq) lo = mid + 1; else hi = mid;
+                        }
+                        for (int32_t j = lo; j < r1 && indices[j] == sq; ++j) av += (double)data[j] * sw[s0 + q];
+                    }
                 }
                 in_seed += av;
                 corr += fabs(av - (1.0 - dmass) * (double)sw[s0 + k]);
@@ -516,7 +537,8 @@ extern "C" int gl_cold_residual(const int32_t* indptr, const int32_t* indices, c
                                 int32_t K, float alpha, double* out, cudaStream_t stream) {
     GL_REQUIRE(n >= 0 && K >= 0, GL_ERR_INVALID_ARGUMENT, "negative size");
     if (K == 0) return GL_OK;
-    GL_REQUIRE(indptr && colsum && seed_ptr && out, GL_ERR_INVALID_ARGUMENT, "a required pointer is NULL");
+    GL_REQUIRE(indptr && indices && data && colsum && seed_ptr && seed_rows && seed_weights && out,
+               GL_ERR_INVALID_ARGUMENT, "a required pointer is NULL");
     cold_residual_kernel<<<grid_for(ceil_div((int64_t)K * 32, kThreads), 8), kThreads, 0, stream>>>(
         indptr, indices, data, colsum, dangling_bits, n, seed_ptr, seed_rows, seed_weights, K, alpha, out);
     GL_LAUNCH_CHECK("cold_residual_kernel");

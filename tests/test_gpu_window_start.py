@@ -127,7 +127,10 @@ def test_cold_residuals_are_exact(device):
     dangling = np.asarray(A.sum(axis=0)).ravel() == 0
     eng = PPREngine(A, block_size=4, device=device, dangling=dangling)
     ws = WindowStart(eng, leaves=1)
-    sets = [np.array([11]), np.array([11, 12, 13]), np.array([64, 65, 66, 67, 64]), np.arange(0, 2048, 61)]
+    # small sets look each seed up in the seed rows; the all-nodes set walks
+    # the rows and looks their columns up in the seed list
+    sets = [np.array([11]), np.array([11, 12, 13]), np.array([64, 65, 66, 67, 64]), np.arange(0, 2048, 61),
+            np.arange(2048)]
     r = ws.cold_residuals(sets, 0.85)
     V = oppr.teleport_matrix(g.n, [np.unique(s) for s in sets])
     ref = ows.cold_residual(A, V, 0.85, dangling)
