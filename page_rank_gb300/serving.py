@@ -108,7 +108,7 @@ class _Group:
             else:
                 x0 = x_keep
                 pre = None
-            run.init(x0)
+            run.init(x0, adopt=True)        # x0 was built here (or gathered from the last run)
         if pre is not None:
             # iterations the start already took, per joining column: a device
             # tensor, read at the next harvest (which waits for the stream)
