@@ -172,8 +172,29 @@ __device__ __forceinline__ void store_out(S* p, const Pack<S, V>& v) {
 #ifndef GL_GATHER_LOAD
 #define GL_GATHER_LOAD 0
 #endif
-template <typename S, int V>
+// SpMM gathers (KEEP): the gathered X rows are marked to stay in L2 before
+// other lines (evict_last).  The SpMM's X (268 MB at the 2^20 / 64-column
+// shape) is reused row by row across stripes: 0.5634 -> 0.5572 ms.  The
+// power-iteration step keeps plain loads: its iterate is many times the L2
+// and the same hint made the 256-column step on 2^22 nodes 5 % slower.
+#ifndef GL_SPMM_X_EVICT_LAST
+#define GL_SPMM_X_EVICT_LAST 1
+#endif
+template <typename S, int V, bool KEEP = false>
 __device__ __forceinline__ Pack<S, V> gather_pack(const S* p) {
+    if constexpr (KEEP && GL_SPMM_X_EVICT_LAST && GL_GATHER_LOAD == 0 && sizeof(S) == 4 && (V == 4 || V == 2)) {
+        unsigned long long pol;
+        asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+        Pack<S, V> r;
+        if constexpr (V == 4) {
+            asm volatile("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+                         : "=f"(r.v[0]), "=f"(r.v[1]), "=f"(r.v[2]), "=f"(r.v[3]) : "l"(p), "l"(pol));
+        } else {
+            asm volatile("ld.global.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
+                         : "=f"(r.v[0]), "=f"(r.v[1]) : "l"(p), "l"(pol));
+        }
+        return r;
+    }
 #if GL_GATHER_LOAD == 1
     Pack<S, V> r;
     if constexpr (sizeof(S) * V == 16) {
@@ -280,7 +301,7 @@ __device__ __forceinline__ int32_t entry_index(const Entry<double>& e) { return 
 // NB gathers (entries e, e + P, ..., all issued before the first FMA) into
 // the lane's V accumulators.  Lanes past the last column gather from a
 // clamped (valid) address and never store.
-template <typename S, int V, int P, int NB>
+template <typename S, int V, int P, int NB, bool KEEP>
 __device__ __forceinline__ void gather_batch(S (&t)[V], const Entry<S>* lst, int e, const S* __restrict__ Xb,
                                              int32_t K) {
     Pack<S, V> x[NB];
@@ -291,8 +312,8 @@ __device__ __forceinline__ void gather_batch(S (&t)[V], const Entry<S>* lst, int
 #pragma unroll
         for (int q = 0; q < NB; q += 2) {
             const int4 c = w[q / 2];
-            x[q] = gather_pack<S, V>(Xb + (long long)c.x * K);
-            x[q + 1] = gather_pack<S, V>(Xb + (long long)c.z * K);
+            x[q] = gather_pack<S, V, KEEP>(Xb + (long long)c.x * K);
+            x[q + 1] = gather_pack<S, V, KEEP>(Xb + (long long)c.z * K);
         }
 #pragma unroll
         for (int q = 0; q < NB; q += 2) {
@@ -305,7 +326,7 @@ __device__ __forceinline__ void gather_batch(S (&t)[V], const Entry<S>* lst, int
         }
     } else {
 #pragma unroll
-        for (int q = 0; q < NB; ++q) x[q] = gather_pack<S, V>(Xb + (long long)lst[e + q * P].col * K);
+        for (int q = 0; q < NB; ++q) x[q] = gather_pack<S, V, KEEP>(Xb + (long long)lst[e + q * P].col * K);
 #pragma unroll
         for (int q = 0; q < NB; ++q) {
             const S v = lst[e + q * P].val;
@@ -319,13 +340,13 @@ __device__ __forceinline__ void gather_batch(S (&t)[V], const Entry<S>* lst, int
 // entries): main batches while they fill, then tail batches.  With P = 2 the
 // two half-warps take alternate entries (each half-warp covers the whole
 // column tile with V-wide loads).
-template <typename S, int V, int P>
+template <typename S, int V, int P, bool KEEP>
 __device__ __forceinline__ void consume_list(S (&t)[V], const Entry<S>* lst, int n_padded,
                                              const S* __restrict__ Xb, int32_t K, int p_lane) {
     constexpr int NG = Gather<S, V>::n;
     int e = p_lane;
-    for (; e + (NG - 1) * P < n_padded; e += NG * P) gather_batch<S, V, P, NG>(t, lst, e, Xb, K);
-    for (; e < n_padded; e += kTail * P) gather_batch<S, V, P, kTail>(t, lst, e, Xb, K);
+    for (; e + (NG - 1) * P < n_padded; e += NG * P) gather_batch<S, V, P, NG, KEEP>(t, lst, e, Xb, K);
+    for (; e < n_padded; e += kTail * P) gather_batch<S, V, P, kTail, KEEP>(t, lst, e, Xb, K);
 }
 
 // Pads the list [0, n) with (0, 0) entries up to a multiple of GR (never
@@ -440,7 +461,7 @@ __device__ __forceinline__ void consume_narrow(const Entry<S>* lst, int n, const
 // list-sized pieces).  The rows are consumed one at a time (each padded to
 // kTail * P entries) into a V-wide accumulator per lane; with P == 2 the two
 // half-warps take alternate entries and are folded by one shuffle per row.
-template <typename S, int BR, int BC, int V, int P>
+template <typename S, int BR, int BC, int V, int P, bool KEEP>
 __device__ __forceinline__ void accumulate_rows(const StripeArgs<S>& a, S* tile, Entry<S>* lst, int32_t* rowinfo,
                                                 int64_t s, int32_t b0, int32_t b1, int32_t j0, int32_t j1,
                                                 const S* __restrict__ Xb, bool lane_ok, int lane, int p_lane,
@@ -714,7 +735,7 @@ __device__ __forceinline__ void accumulate_rows(const StripeArgs<S>& a, S* tile,
                 if constexpr (NARROW) {
                     consume_narrow<S, BR, 32 / P>(lst + base, n, nullptr, r, tile, c_lane, p_lane, lane_ok, Xb, a.K);
                 } else {
-                    consume_list<S, V, P>(t, lst + base, n, Xb, a.K, p_lane);
+                    consume_list<S, V, P, KEEP>(t, lst + base, n, Xb, a.K, p_lane);
                 }
                 if (rs >= re) break;
                 __syncwarp();
@@ -1083,7 +1104,7 @@ stripe_kernel(const StripeArgs<S> a) {
         // lanes past the last column read a valid address and never store
         const S* __restrict__ Xb = a.X + b * a.cols * (int64_t)a.K + (lane_ok ? col_base : 0);
 
-        accumulate_rows<S, BR, BC, V, P>(a, otile, lst, rowinfo, s, b0, b1, j0, j1, Xb, lane_ok, lane, p_lane,
+        accumulate_rows<S, BR, BC, V, P, !PPR>(a, otile, lst, rowinfo, s, b0, b1, j0, j1, Xb, lane_ok, lane, p_lane,
                                          c_lane, rp_known, rp);
         // from here on lane (c_lane, p_lane == 0) owns columns [c_lane * V, +V)
         // of every tile row
