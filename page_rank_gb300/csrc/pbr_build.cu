@@ -8,6 +8,10 @@
 // rows by block column (warp-min of the lanes' head block columns), which
 // yields the stripe's distinct blocks in block-column order together with
 // their bitmask, the CSR position of their first nonzero, and per-row counts.
+// Warps draw their stripes from a counter.  Long stripes (more than
+// kBigCountEntries entries to count, more than kSmallStripeBlocks distinct
+// blocks to order) go to 1024-thread CTAs instead, which sort instead of
+// merging; the count pass lists them for those kernels, hub stripes first.
 //
 // Three device passes:
 //   count  — per stripe: distinct / kept blocks, packed values; per row:
@@ -57,9 +61,29 @@ constexpr int64_t kInf = INT64_MAX;
 
 enum BuildFlag { kFlagRange = 0, kFlagNoncanon = 1, kFlagIndptr = 2, kNumFlags = 4 };
 
+// Work lists of the CTA kernels.  The count pass lists the stripes that go to
+// build_count_big_kernel and to build_fill_big_kernel; each list fills from
+// the front with its huge stripes (more than kHugeEntries entries: R-MAT hub
+// rows) and from the back with the others, and the CTAs draw from it through
+// a counter, so the huge stripes start first and no CTA is left holding a
+// run of hub stripes that a static stride gave it.  The draw order does not
+// change the output: every stripe writes to places fixed by the scans.
+enum BuildWork {
+    kWorkCountHead = 0, kWorkCountTail = 1, kWorkCountDraw = 2,
+    kWorkFillHead = 3, kWorkFillTail = 4, kWorkFillDraw = 5, kWorkFillWarpDraw = 6, kWorkCountWarpDraw = 7,
+    kNumWork = 8
+};
+constexpr int64_t kHugeEntries = 4096;
+// Stripes with up to this many distinct blocks are ordered by one warp
+// (build_fill_kernel), bigger ones by a CTA (build_fill_big_kernel).
+constexpr int kSmallStripeBlocks = 64;
+
 // Workspace layout (every region 256-byte aligned).
 struct BuildWs {
     int32_t* flags;         // kNumFlags
+    int32_t* work;          // kNumWork: list heads / tails and draw counters
+    int32_t* count_list;    // nstripes: stripes for build_count_big_kernel
+    int32_t* fill_list;     // nstripes: stripes for build_fill_big_kernel
     int64_t* stripe_m;      // nstripes + 1 : distinct blocks   -> exclusive scan
     int64_t* stripe_kept;   // nstripes + 1 : kept blocks       -> exclusive scan
     int64_t* stripe_packed; // nstripes + 1 : kept values       -> exclusive scan
@@ -100,6 +124,9 @@ BuildWs layout_ws(void* base, int64_t rows, int64_t nnz, int32_t br) {
     int64_t off = 0;
     auto take = [&](int64_t bytes) { char* q = p ? p + off : nullptr; off += align256(bytes); return q; };
     w.flags = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * kNumFlags));
+    w.work = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * kNumWork));
+    w.count_list = reinterpret_cast<int32_t*>(take(4 * (ns > 0 ? ns : 1)));
+    w.fill_list = reinterpret_cast<int32_t*>(take(4 * (ns > 0 ? ns : 1)));
     w.stripe_m = reinterpret_cast<int64_t*>(take(8 * (ns + 1)));
     w.stripe_kept = reinterpret_cast<int64_t*>(take(8 * (ns + 1)));
     w.stripe_packed = reinterpret_cast<int64_t*>(take(8 * (ns + 1)));
@@ -173,7 +200,9 @@ struct StripeMerge {
         prev_col = -1;
     }
 
-    // Returns false when the stripe is exhausted.
+    // Returns false when the stripe is exhausted.  FIRST: also reduce the
+    // block's first CSR position over the warp.
+    template <bool FIRST = true>
     __device__ bool step(int64_t cols, int64_t& bcol, uint64_t& code, int64_t& first,
                          int& my_count, int64_t& my_first) {
         const int64_t head = (p < end) ? (int64_t)indices[p] / bc : kInf;
@@ -200,7 +229,7 @@ struct StripeMerge {
         }
         bcol = cur;
         code = warp_or_u64(bits);
-        first = warp_min_i64(f);
+        first = FIRST ? warp_min_i64(f) : f;
         my_count = cnt;
         my_first = f;
         return true;
@@ -219,8 +248,85 @@ __device__ __forceinline__ int64_t stripe_entries(const I* indptr, int64_t s, in
 }
 
 // Stripes with more entries than this are counted by a whole CTA
-// (build_count_big_kernel) instead of one warp's serial merge.
-constexpr int64_t kBigCountEntries = 2048;
+// (build_count_big_kernel) instead of one warp's serial merge, whose time
+// grows with the stripe's distinct blocks (one merge step each).  256 was the
+// fastest of 128 / 256 / 384 / 512 / 2048 on a 2^20-row R-MAT graph.
+#ifndef GL_BUILD_BIG_COUNT_ENTRIES
+#define GL_BUILD_BIG_COUNT_ENTRIES 256
+#endif
+constexpr int64_t kBigCountEntries = GL_BUILD_BIG_COUNT_ENTRIES;
+
+// Stripes the CTA kernels handle with at most this many entries keep their
+// per-entry and per-block scratch in dynamic shared memory instead of the
+// global workspace (each of their ~100 dependent passes then waits on
+// shared-memory latency, not L2).  0 keeps all scratch global.
+#ifndef GL_BUILD_SMEM_ENTRIES
+#define GL_BUILD_SMEM_ENTRIES 1024
+#endif
+constexpr int kSmemEntries = GL_BUILD_SMEM_ENTRIES;
+// Resident 1024-thread CTAs per SM the two CTA kernels are compiled for (and
+// launched with): the count kernel keeps 64 registers (at 32 it spills and
+// was 6 % slower), the fill kernel runs two CTAs per SM on 1024-entry shared
+// scratch (faster than one CTA on 1536 or 2048 entries).
+#ifndef GL_BUILD_COUNT_BIG_CTAS
+#define GL_BUILD_COUNT_BIG_CTAS 1
+#endif
+#ifndef GL_BUILD_FILL_BIG_CTAS
+#define GL_BUILD_FILL_BIG_CTAS 2
+#endif
+
+// Hands a warp its stripes: GL_BUILD_WARP_DRAW consecutive stripes per draw
+// from a counter, so warps that drew cheap stripes come back for more (one
+// per draw was fastest; a static stride over the grid's warps, 0, left warps
+// waiting on a neighbour's run of long stripes).
+#ifndef GL_BUILD_WARP_DRAW
+#define GL_BUILD_WARP_DRAW 1
+#endif
+struct WarpDraw {
+    int32_t* counter;
+    int64_t ns, s, end;
+    __device__ WarpDraw(int32_t* c, int64_t n) : counter(c), ns(n), s(-1), end(-1) {}
+    __device__ bool next() {
+#if GL_BUILD_WARP_DRAW > 0
+        if (++s >= end) {
+            int b = 0;
+            if ((threadIdx.x & 31) == 0) b = atomicAdd(counter, GL_BUILD_WARP_DRAW);
+            b = __shfl_sync(0xffffffffu, b, 0);
+            s = b;
+            end = (int64_t)b + GL_BUILD_WARP_DRAW;
+        }
+#else
+        const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+        s = s < 0 ? (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5) : s + nw;
+#endif
+        return s < ns;
+    }
+};
+
+// Appends stripe s to a work list (head slot `slot`, tail slot `slot + 1`).
+__device__ __forceinline__ void list_push(int32_t* list, int32_t* work, int slot, int64_t ns, int64_t s, bool huge) {
+    if (huge) list[atomicAdd(&work[slot], 1)] = (int32_t)s;
+    else list[ns - 1 - atomicAdd(&work[slot + 1], 1)] = (int32_t)s;
+}
+
+// Next stripe of a work list for the calling CTA (huge stripes first), or -1
+// once the list is exhausted.  Called by every thread of the CTA.
+__device__ __forceinline__ int64_t list_draw(const int32_t* list, int32_t* work, int slot, int64_t ns, int* s_item) {
+    if (threadIdx.x == 0) {
+        const int d = atomicAdd(&work[slot + 2], 1);
+        const int h = work[slot], tl = work[slot + 1];
+        *s_item = d < h ? list[d] : (d - h < tl ? list[ns - 1 - (d - h)] : -1);
+    }
+    __syncthreads();
+    const int64_t s = *s_item;
+    __syncthreads();
+    return s;
+}
+// count: four int32 arrays per entry
+constexpr int kCountSmemBytes = 16 * kSmemEntries;
+// fill: four int32 arrays per entry; per block (at most one per entry) two
+// 64-bit and ten int32 arrays
+constexpr int kFillSmemBytes = 16 * kSmemEntries + 56 * kSmemEntries;
 
 // ---------------------------------------------------------------------------
 // count: per stripe distinct / kept blocks and kept values; per row remainder
@@ -231,10 +337,13 @@ __global__ void __launch_bounds__(kBuildThreads)
 build_count_kernel(const I* indptr, const I* indices, int64_t rows, int64_t cols, int64_t nnz, int br, int bc,
                    int min_nnz, int64_t nstripes, BuildWs w) {
     const int lane = threadIdx.x & 31;
-    const int64_t warp_id = (int64_t)blockIdx.x * kBuildWarps + (threadIdx.x >> 5);
-    const int64_t nwarps = (int64_t)gridDim.x * kBuildWarps;
-    for (int64_t s = warp_id; s < nstripes; s += nwarps) {
-        if (stripe_entries(indptr, s, rows, nnz, br) > kBigCountEntries) continue;   // build_count_big_kernel
+    for (WarpDraw d(&w.work[kWorkCountWarpDraw], nstripes); d.next();) {
+        const int64_t s = d.s;
+        const int64_t ent = stripe_entries(indptr, s, rows, nnz, br);
+        if (ent > kBigCountEntries) {   // build_count_big_kernel
+            if (lane == 0) list_push(w.count_list, w.work, kWorkCountHead, nstripes, s, ent > kHugeEntries);
+            continue;
+        }
         StripeMerge<I> mg;
         mg.init(indptr, indices, s, rows, nnz, br, bc, true);
         int64_t m = 0, kept = 0, packed = 0, rem = 0;
@@ -242,7 +351,7 @@ build_count_kernel(const I* indptr, const I* indices, int64_t rows, int64_t cols
         uint64_t code;
         int my_count;
         int64_t last_bcol = -1;
-        while (mg.step(cols, bcol, code, first, my_count, my_first)) {
+        while (mg.template step<false>(cols, bcol, code, first, my_count, my_first)) {
             // A negative or out-of-order column makes block columns repeat;
             // the count is still finite and the flags reject the build.
             if (bcol <= last_bcol) mg.bad_order = 1;
@@ -260,6 +369,7 @@ build_count_kernel(const I* indptr, const I* indices, int64_t rows, int64_t cols
             w.stripe_m[s] = m;
             w.stripe_kept[s] = kept;
             w.stripe_packed[s] = packed;
+            if (m > kSmallStripeBlocks) list_push(w.fill_list, w.work, kWorkFillHead, nstripes, s, ent > kHugeEntries);
         }
         const int64_t row = s * br + lane;
         if (lane < br && row < rows) w.row_rem[row] = rem;
@@ -286,7 +396,6 @@ struct Team<32> {
     static __device__ __forceinline__ void sync() { __syncwarp(); }
 };
 
-constexpr int kSmallStripeBlocks = 64;   // warp team up to this many distinct blocks
 constexpr int kBigThreads = 1024;
 
 // Orders the records with insertion rank < present as the standard library's
@@ -363,7 +472,7 @@ __device__ void move_values(const I* indptr, const I* indices, const S* values, 
     uint64_t code;
     int my_count;
     int j = 0;
-    while (mg.step(cols, bcol, code, first, my_count, my_first)) {
+    while (mg.template step<false>(cols, bcol, code, first, my_count, my_first)) {
         if (slot[j] >= 0) {
             const int before = (int)warp_incl_scan_i64(my_count) - my_count;
             const int64_t dst = packed_base + doff[j] + before;
@@ -679,16 +788,19 @@ __device__ void move_values_big(BigShared& sh, const I* indptr, const I* indices
 // OR-ed together (two 32-bit halves), and kept blocks, packed values and
 // per-row remainder entries are summed.
 template <typename I>
-__global__ void __launch_bounds__(kBigThreads)
+__global__ void __launch_bounds__(kBigThreads, GL_BUILD_COUNT_BIG_CTAS)
 build_count_big_kernel(const I* indptr, const I* indices, int64_t rows, int64_t cols, int64_t nnz, int br, int bc,
                        int min_nnz, int64_t nstripes, int64_t ncb, BuildWs w) {
     __shared__ BigShared sh;
+    extern __shared__ __align__(16) unsigned char build_dyn[];
     __shared__ unsigned long long s_tot[3];   // distinct, kept, packed
     __shared__ int32_t s_rem[33];
     __shared__ int32_t s_bad[3];
+    __shared__ int s_item;
     const int t = threadIdx.x;
-    for (int64_t s = blockIdx.x; s < nstripes; s += gridDim.x) {
-        if (stripe_entries(indptr, s, rows, nnz, br) <= kBigCountEntries) continue;
+    for (;;) {
+        const int64_t s = list_draw(w.count_list, w.work, kWorkCountHead, nstripes, &s_item);
+        if (s < 0) break;
         const int64_t r0 = s * br;
         const int64_t r1 = r0 + br < rows ? r0 + br : rows;
         const int nr = (int)(r1 - r0);
@@ -712,6 +824,10 @@ build_count_big_kernel(const I* indptr, const I* indices, int64_t rows, int64_t 
         }
         __syncthreads();
         BigEntries en{w.ent_a + e0, w.ent_b + e0, w.ent_c + e0, w.ent_d + e0};
+        if (n <= kSmemEntries) {
+            int32_t* d = reinterpret_cast<int32_t*>(build_dyn);
+            en = BigEntries{d, d + kSmemEntries, d + 2 * kSmemEntries, d + 3 * kSmemEntries};
+        }
         for (int i = t; i < n; i += kBigThreads) {
             int64_t col = (int64_t)indices[e0 + i];
             const int r = big_row_of(sh, br, i);
@@ -761,6 +877,8 @@ build_count_big_kernel(const I* indptr, const I* indices, int64_t rows, int64_t 
             w.stripe_m[s] = (int64_t)s_tot[0];
             w.stripe_kept[s] = (int64_t)s_tot[1];
             w.stripe_packed[s] = (int64_t)s_tot[2];
+            if ((int64_t)s_tot[0] > kSmallStripeBlocks)
+                list_push(w.fill_list, w.work, kWorkFillHead, nstripes, s, n > kHugeEntries);
             for (int f = 0; f < 3; ++f)
                 if (s_bad[f]) atomicOr(&w.flags[f], 1);
         }
@@ -890,9 +1008,8 @@ build_fill_kernel(const I* indptr, const I* indices, const S* values, int64_t ro
                   BuildWs w, uint64_t* out_codes, I* out_coords, I* out_offsets, S* out_data,
                   I* out_rem_col, S* out_rem_val, int32_t* out_stripe_ptr) {
     const int lane = threadIdx.x & 31;
-    const int64_t warp_id = (int64_t)blockIdx.x * kBuildWarps + (threadIdx.x >> 5);
-    const int64_t nwarps = (int64_t)gridDim.x * kBuildWarps;
-    for (int64_t s = warp_id; s < nstripes; s += nwarps) {
+    for (WarpDraw d(&w.work[kWorkFillWarpDraw], nstripes); d.next();) {
+        const int64_t s = d.s;
         const int64_t rbase = w.stripe_m[s];
         const int m = (int)(w.stripe_m[s + 1] - rbase);
         const int64_t kept_base = w.stripe_kept[s];
@@ -911,26 +1028,40 @@ build_fill_kernel(const I* indptr, const I* indices, const S* values, int64_t ro
 }
 
 template <typename I, typename S>
-__global__ void __launch_bounds__(kBigThreads)
+__global__ void __launch_bounds__(kBigThreads, GL_BUILD_FILL_BIG_CTAS)
 build_fill_big_kernel(const I* indptr, const I* indices, const S* values, int64_t rows, int64_t cols, int64_t nnz,
                       int br, int bc, int min_nnz, int64_t nstripes, int64_t ncb, bool key32, int nchain,
                       BuildWs w, uint64_t* out_codes, I* out_coords, I* out_offsets, S* out_data,
                       I* out_rem_col, S* out_rem_val) {
     __shared__ BigShared sh;
-    for (int64_t s = blockIdx.x; s < nstripes; s += gridDim.x) {
+    extern __shared__ __align__(16) unsigned char build_dyn[];
+    __shared__ int s_item;
+    for (;;) {
+        const int64_t s = list_draw(w.fill_list, w.work, kWorkFillHead, nstripes, &s_item);
+        if (s < 0) break;
         const int64_t rbase = w.stripe_m[s];
         const int m = (int)(w.stripe_m[s + 1] - rbase);
-        if (m <= kSmallStripeBlocks) continue;
         const int64_t e0 = (int64_t)indptr[s * br];
+        const int64_t r1 = (s + 1) * br < rows ? (s + 1) * br : rows;
+        const int64_t n = (int64_t)indptr[r1] - e0;
         BigEntries en{w.ent_a + e0, w.ent_b + e0, w.ent_c + e0, w.ent_d + e0};
-        record_blocks_big<I>(sh, indptr, indices, s, rows, br, bc, ncb, en, w.rec_code + rbase, w.rec_bcol + rbase,
-                             w.rec_ins + rbase);
         BigRecs r{w.rec_code + rbase, w.rec_bcol + rbase, w.rec_ins + rbase, w.rec_tau + rbase,
                   w.rec_bkt + rbase, w.rec_g + rbase, w.rec_pos + rbase, w.rec_pops + rbase,
                   w.rec_k0 + rbase, w.rec_v0 + rbase, w.rec_k1 + rbase, w.rec_v1 + rbase};
+        if (n <= kSmemEntries) {   // m <= n: every block holds an entry
+            constexpr int K = kSmemEntries;
+            uint64_t* d64 = reinterpret_cast<uint64_t*>(build_dyn);
+            int32_t* d32 = reinterpret_cast<int32_t*>(d64 + 2 * K);
+            en = BigEntries{d32, d32 + K, d32 + 2 * K, d32 + 3 * K};
+            int32_t* q = d32 + 4 * K;
+            r = BigRecs{d64, reinterpret_cast<int64_t*>(d64 + K), q, q + K, reinterpret_cast<uint32_t*>(q + 2 * K),
+                        q + 3 * K, q + 4 * K, q + 5 * K, q + 6 * K, q + 7 * K, q + 8 * K, q + 9 * K};
+        }
+        record_blocks_big<I>(sh, indptr, indices, s, rows, br, bc, ncb, en, const_cast<uint64_t*>(r.code),
+                             const_cast<int64_t*>(r.bcol), r.ins);
         order_stripe_big<I>(sh, s, m, br, bc, min_nnz, ncb, key32, nchain, w.chain, w.stripe_prefmax[s],
                             w.stripe_kept[s], w.stripe_packed[s], r, out_codes, out_coords, out_offsets);
-        move_values_big<I, S>(sh, indptr, indices, values, s, rows, br, en, w.rec_tau + rbase, w.rec_g + rbase,
+        move_values_big<I, S>(sh, indptr, indices, values, s, rows, br, en, r.tau, r.g,
                               w.stripe_packed[s], w.row_rem, out_data, out_rem_col, out_rem_val);
     }
 }
@@ -953,6 +1084,7 @@ int check_args(int32_t index_type, int64_t rows, int64_t cols, int64_t nnz, int3
     GL_REQUIRE(br >= 1 && bc >= 1 && (int64_t)br * bc <= 64, GL_ERR_INVALID_ARGUMENT,
                "block_rows * block_cols must be in 1..64 (got %d x %d)", br, bc);
     GL_REQUIRE(br <= 32, GL_ERR_INVALID_ARGUMENT, "block_rows > 32 is not supported by the device builder");
+    GL_REQUIRE(ceil_div(rows, br) < (int64_t)(INT32_MAX / 2), GL_ERR_INVALID_ARGUMENT, "too many stripes for int32 stripe lists");
     GL_REQUIRE(min_nnz >= 0 && min_nnz <= 255, GL_ERR_INVALID_ARGUMENT, "min_nnz_per_block must be in 0..255");
     GL_REQUIRE(nnz < (int64_t)INT32_MAX || index_type == GL_I64, GL_ERR_INVALID_ARGUMENT,
                "nnz does not fit the int32 index type");
@@ -987,6 +1119,7 @@ int count_impl(const I* indptr, const I* indices, int64_t rows, int64_t cols, in
                int32_t min_nnz, const BuildWs& w, gl_pbr_build_counts* counts, cudaStream_t stream) {
     const int64_t ns = ceil_div(rows, br);
     GL_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int32_t) * kNumFlags, stream));
+    GL_CUDA_TRY(cudaMemsetAsync(w.work, 0, sizeof(int32_t) * kNumWork, stream));
     {
         // The trailing slot of every count array must be zero for the scans.
         int64_t* regions[5] = {w.stripe_m, w.stripe_kept, w.stripe_packed, w.stripe_prefmax, w.row_rem};
@@ -1001,10 +1134,22 @@ int count_impl(const I* indptr, const I* indices, int64_t rows, int64_t cols, in
                                                                               bc, min_nnz, ns, w);
         GL_LAUNCH_CHECK("build_count_kernel");
         const int64_t ncb = ceil_div(cols, bc);
-        int64_t big_blocks = (int64_t)num_sms() * 2;
+        int64_t big_blocks = (int64_t)num_sms() * GL_BUILD_COUNT_BIG_CTAS;
         if (big_blocks > ns) big_blocks = ns;
-        build_count_big_kernel<I><<<(unsigned)big_blocks, kBigThreads, 0, stream>>>(indptr, indices, rows, cols, nnz,
-                                                                                    br, bc, min_nnz, ns, ncb, w);
+        static std::atomic<int> attr_cache[kMaxDevices];
+        int attr = 0;
+        const int arc = per_device_value(
+            attr_cache,
+            [&](int* v) {
+                GL_CUDA_TRY(cudaFuncSetAttribute(build_count_big_kernel<I>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 kCountSmemBytes));
+                *v = 1;
+                return GL_OK;
+            },
+            &attr);
+        if (arc != GL_OK) return arc;
+        build_count_big_kernel<I><<<(unsigned)big_blocks, kBigThreads, kCountSmemBytes, stream>>>(
+            indptr, indices, rows, cols, nnz, br, bc, min_nnz, ns, ncb, w);
         GL_LAUNCH_CHECK("build_count_big_kernel");
     }
     int rc;
@@ -1063,6 +1208,8 @@ int fill_impl(const I* indptr, const I* indices, const S* values, int64_t rows, 
     GL_REQUIRE(nchain > 0, GL_ERR_INVALID_ARGUMENT, "bucket chain longer than %d steps", kMaxChain);
     GL_CUDA_TRY(cudaMemcpyAsync(w.chain, chain, sizeof(int64_t) * 2 * nchain, cudaMemcpyHostToDevice, stream));
     if (ns > 0) {
+        // the fill's draw counters are reset here, so a fill may be repeated after one count
+        GL_CUDA_TRY(cudaMemsetAsync(w.work + kWorkFillDraw, 0, 2 * sizeof(int32_t), stream));
         int64_t blocks = ceil_div(ns, kBuildWarps);
         const int64_t cap = (int64_t)num_sms() * 16;
         if (blocks > cap) blocks = cap;
@@ -1071,8 +1218,21 @@ int fill_impl(const I* indptr, const I* indices, const S* values, int64_t rows, 
             coords, offsets, data, rem_col, rem_val, stripe_ptr);
         GL_LAUNCH_CHECK("build_fill_kernel");
         if (counts->max_stripe_blocks > kSmallStripeBlocks) {
-            const int64_t big_blocks = (int64_t)num_sms() * 2;
-            build_fill_big_kernel<I, S><<<(unsigned)big_blocks, kBigThreads, 0, stream>>>(
+            int64_t big_blocks = (int64_t)num_sms() * GL_BUILD_FILL_BIG_CTAS;
+            if (big_blocks > ns) big_blocks = ns;
+            static std::atomic<int> attr_cache[kMaxDevices];
+            int attr = 0;
+            const int arc = per_device_value(
+                attr_cache,
+                [&](int* v) {
+                    GL_CUDA_TRY(cudaFuncSetAttribute(build_fill_big_kernel<I, S>,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kFillSmemBytes));
+                    *v = 1;
+                    return GL_OK;
+                },
+                &attr);
+            if (arc != GL_OK) return arc;
+            build_fill_big_kernel<I, S><<<(unsigned)big_blocks, kBigThreads, kFillSmemBytes, stream>>>(
                 indptr, indices, values, rows, cols, nnz, br, bc, min_nnz, ns, (int64_t)ncb, sizeof(I) == 4, nchain,
                 w, codes, coords, offsets, data, rem_col, rem_val);
             GL_LAUNCH_CHECK("build_fill_big_kernel");
