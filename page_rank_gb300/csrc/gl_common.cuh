@@ -88,16 +88,17 @@ inline int num_sms() {
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 // Warp-wide reductions.
-// Exact 64-bit minimum with two 32-bit warp reductions (redux.sync): the
-// high words as signed, then the low words as unsigned among the lanes that
-// hold the smallest high word.
-__device__ __forceinline__ int64_t warp_min_i64(int64_t v) {
+// Exact 64-bit minimum over the lanes of `mask` with two 32-bit reductions
+// (redux.sync): the high words as signed, then the low words as unsigned
+// among the lanes that hold the smallest high word.
+__device__ __forceinline__ int64_t group_min_i64(int64_t v, unsigned mask) {
     const int hi = (int)(v >> 32);
-    const int mhi = __reduce_min_sync(0xffffffffu, hi);
+    const int mhi = __reduce_min_sync(mask, hi);
     const unsigned lo = hi == mhi ? (unsigned)(uint64_t)v : 0xffffffffu;
-    const unsigned mlo = __reduce_min_sync(0xffffffffu, lo);
+    const unsigned mlo = __reduce_min_sync(mask, lo);
     return (int64_t)(((uint64_t)(uint32_t)mhi << 32) | mlo);
 }
+__device__ __forceinline__ int64_t warp_min_i64(int64_t v) { return group_min_i64(v, 0xffffffffu); }
 __device__ __forceinline__ int64_t warp_max_i64(int64_t v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -106,11 +107,12 @@ __device__ __forceinline__ int64_t warp_max_i64(int64_t v) {
     }
     return v;
 }
-__device__ __forceinline__ uint64_t warp_or_u64(uint64_t v) {
-    const unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)v);
-    const unsigned hi = __reduce_or_sync(0xffffffffu, (unsigned)(v >> 32));
+__device__ __forceinline__ uint64_t group_or_u64(uint64_t v, unsigned mask) {
+    const unsigned lo = __reduce_or_sync(mask, (unsigned)v);
+    const unsigned hi = __reduce_or_sync(mask, (unsigned)(v >> 32));
     return ((uint64_t)hi << 32) | lo;
 }
+__device__ __forceinline__ uint64_t warp_or_u64(uint64_t v) { return group_or_u64(v, 0xffffffffu); }
 __device__ __forceinline__ int warp_sum_i32(int v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

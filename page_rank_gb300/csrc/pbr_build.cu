@@ -161,13 +161,21 @@ BuildWs layout_ws(void* base, int64_t rows, int64_t nnz, int32_t br) {
 // (for every lane) the block column, the lane's first position and count in
 // that block, and the block's code / first position over the whole stripe.
 // ---------------------------------------------------------------------------
-template <typename I>
+// G: lanes per stripe (a power of two >= block_rows); a warp merges 32 / G
+// stripes at once, each group of G lanes with its own reductions.
+template <int G>
+__device__ __forceinline__ unsigned group_mask() {
+    return G == 32 ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+}
+
+template <typename I, int G = 32>
 struct StripeMerge {
     const I* indices;
     int64_t p, end;          // this lane's cursor into its row
     int64_t row_start;
     int64_t prev_col;
-    int br, bc, lane;
+    int br, bc, lane;        // lane: this thread's row within the stripe
+    unsigned gmask;
     bool check;
     int bad_range, bad_order, bad_indptr;
 
@@ -178,7 +186,8 @@ struct StripeMerge {
         indices = idx;
         br = br_;
         bc = bc_;
-        lane = threadIdx.x & 31;
+        lane = threadIdx.x & (G - 1);
+        gmask = group_mask<G>();
         check = chk;
         bad_range = 0;
         bad_order = 0;
@@ -206,7 +215,7 @@ struct StripeMerge {
     __device__ bool step(int64_t cols, int64_t& bcol, uint64_t& code, int64_t& first,
                          int& my_count, int64_t& my_first) {
         const int64_t head = (p < end) ? (int64_t)indices[p] / bc : kInf;
-        const int64_t cur = warp_min_i64(head);
+        const int64_t cur = group_min_i64(head, gmask);
         if (cur == kInf) return false;
         uint64_t bits = 0;
         int cnt = 0;
@@ -228,8 +237,8 @@ struct StripeMerge {
             }
         }
         bcol = cur;
-        code = warp_or_u64(bits);
-        first = FIRST ? warp_min_i64(f) : f;
+        code = group_or_u64(bits, gmask);
+        first = FIRST ? group_min_i64(f, gmask) : f;
         my_count = cnt;
         my_first = f;
         return true;
@@ -282,6 +291,7 @@ constexpr int kSmemEntries = GL_BUILD_SMEM_ENTRIES;
 #ifndef GL_BUILD_WARP_DRAW
 #define GL_BUILD_WARP_DRAW 1
 #endif
+template <int G = 32>
 struct WarpDraw {
     int32_t* counter;
     int64_t ns, s, end;
@@ -289,15 +299,18 @@ struct WarpDraw {
     __device__ bool next() {
 #if GL_BUILD_WARP_DRAW > 0
         if (++s >= end) {
+            const int lead = (threadIdx.x & 31) & ~(G - 1);
             int b = 0;
-            if ((threadIdx.x & 31) == 0) b = atomicAdd(counter, GL_BUILD_WARP_DRAW);
-            b = __shfl_sync(0xffffffffu, b, 0);
+            if ((threadIdx.x & 31) == lead) b = atomicAdd(counter, GL_BUILD_WARP_DRAW);
+            b = __shfl_sync(group_mask<G>(), b, lead);
             s = b;
             end = (int64_t)b + GL_BUILD_WARP_DRAW;
         }
 #else
-        const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-        s = s < 0 ? (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5) : s + nw;
+        constexpr int kGroups = 32 / G;
+        const int64_t ng = (int64_t)gridDim.x * (blockDim.x >> 5) * kGroups;
+        s = s < 0 ? ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * kGroups + ((threadIdx.x & 31) / G)
+                  : s + ng;
 #endif
         return s < ns;
     }
@@ -332,19 +345,21 @@ constexpr int kFillSmemBytes = 16 * kSmemEntries + 56 * kSmemEntries;
 // count: per stripe distinct / kept blocks and kept values; per row remainder
 // entries; validation flags.
 // ---------------------------------------------------------------------------
-template <typename I>
+// G lanes per stripe (block_rows <= G), 32 / G stripes per warp at a time.
+template <typename I, int G>
 __global__ void __launch_bounds__(kBuildThreads)
 build_count_kernel(const I* indptr, const I* indices, int64_t rows, int64_t cols, int64_t nnz, int br, int bc,
                    int min_nnz, int64_t nstripes, BuildWs w) {
-    const int lane = threadIdx.x & 31;
-    for (WarpDraw d(&w.work[kWorkCountWarpDraw], nstripes); d.next();) {
+    const int lane = threadIdx.x & (G - 1);
+    const unsigned gmask = group_mask<G>();
+    for (WarpDraw<G> d(&w.work[kWorkCountWarpDraw], nstripes); d.next();) {
         const int64_t s = d.s;
         const int64_t ent = stripe_entries(indptr, s, rows, nnz, br);
         if (ent > kBigCountEntries) {   // build_count_big_kernel
             if (lane == 0) list_push(w.count_list, w.work, kWorkCountHead, nstripes, s, ent > kHugeEntries);
             continue;
         }
-        StripeMerge<I> mg;
+        StripeMerge<I, G> mg;
         mg.init(indptr, indices, s, rows, nnz, br, bc, true);
         int64_t m = 0, kept = 0, packed = 0, rem = 0;
         int64_t bcol, first, my_first;
@@ -373,9 +388,9 @@ build_count_kernel(const I* indptr, const I* indices, int64_t rows, int64_t cols
         }
         const int64_t row = s * br + lane;
         if (lane < br && row < rows) w.row_rem[row] = rem;
-        if (__any_sync(0xffffffffu, mg.bad_range) && lane == 0) atomicOr(&w.flags[kFlagRange], 1);
-        if (__any_sync(0xffffffffu, mg.bad_order) && lane == 0) atomicOr(&w.flags[kFlagNoncanon], 1);
-        if (__any_sync(0xffffffffu, mg.bad_indptr) && lane == 0) atomicOr(&w.flags[kFlagIndptr], 1);
+        if (__any_sync(gmask, mg.bad_range) && lane == 0) atomicOr(&w.flags[kFlagRange], 1);
+        if (__any_sync(gmask, mg.bad_order) && lane == 0) atomicOr(&w.flags[kFlagNoncanon], 1);
+        if (__any_sync(gmask, mg.bad_indptr) && lane == 0) atomicOr(&w.flags[kFlagIndptr], 1);
     }
 }
 
@@ -1094,7 +1109,7 @@ int check_args(int32_t index_type, int64_t rows, int64_t cols, int64_t nnz, int3
 // Bucket counts the standard library's unordered_map goes through when built
 // with `hint` buckets and filled one key at a time, as (count, buckets) pairs;
 // the first pair is (0, initial buckets).
-int bucket_chain(uint64_t hint, int64_t max_elems, int64_t* pairs) {
+int bucket_chain_probe(uint64_t hint, int64_t max_elems, int64_t* pairs) {
     std::unordered_map<int64_t, uint8_t> probe(static_cast<size_t>(hint));
     int n = 0;
     size_t last = probe.bucket_count();
@@ -1110,6 +1125,37 @@ int bucket_chain(uint64_t hint, int64_t max_elems, int64_t* pairs) {
             pairs[2 * n + 1] = (int64_t)last;
             ++n;
         }
+    }
+    return n;
+}
+
+// bucket_chain_probe, remembered per hint: the chain for fewer elements is a
+// prefix of the chain for more, so the longest one probed so far answers
+// every request up to its length (a 17 k-element probe costs the host about
+// a millisecond per build otherwise).
+int bucket_chain(uint64_t hint, int64_t max_elems, int64_t* pairs) {
+    struct Chain {
+        int64_t upto = -1;
+        int n = 0;
+        int64_t pairs[2 * kMaxChain];
+    };
+    static std::unordered_map<uint64_t, Chain> cache;
+    std::lock_guard<std::mutex> lock(setup_mutex());
+    Chain& c = cache[hint];
+    if (c.upto < max_elems) {
+        const int n = bucket_chain_probe(hint, max_elems, c.pairs);
+        if (n < 0) {
+            c.upto = -1;
+            return -1;
+        }
+        c.n = n;
+        c.upto = max_elems;
+    }
+    int n = 0;
+    while (n < c.n && c.pairs[2 * n] <= max_elems) {
+        pairs[2 * n] = c.pairs[2 * n];
+        pairs[2 * n + 1] = c.pairs[2 * n + 1];
+        ++n;
     }
     return n;
 }
@@ -1130,8 +1176,18 @@ int count_impl(const I* indptr, const I* indices, int64_t rows, int64_t cols, in
         int64_t blocks = ceil_div(ns, kBuildWarps);
         const int64_t cap = (int64_t)num_sms() * 16;
         if (blocks > cap) blocks = cap;
-        build_count_kernel<I><<<(unsigned)blocks, kBuildThreads, 0, stream>>>(indptr, indices, rows, cols, nnz, br,
-                                                                              bc, min_nnz, ns, w);
+#ifndef GL_BUILD_COUNT_GROUP
+#define GL_BUILD_COUNT_GROUP 8
+#endif
+        if (br <= 8 && GL_BUILD_COUNT_GROUP <= 8)
+            build_count_kernel<I, 8><<<(unsigned)blocks, kBuildThreads, 0, stream>>>(indptr, indices, rows, cols, nnz,
+                                                                                     br, bc, min_nnz, ns, w);
+        else if (br <= 16 && GL_BUILD_COUNT_GROUP <= 16)
+            build_count_kernel<I, 16><<<(unsigned)blocks, kBuildThreads, 0, stream>>>(indptr, indices, rows, cols,
+                                                                                      nnz, br, bc, min_nnz, ns, w);
+        else
+            build_count_kernel<I, 32><<<(unsigned)blocks, kBuildThreads, 0, stream>>>(indptr, indices, rows, cols,
+                                                                                      nnz, br, bc, min_nnz, ns, w);
         GL_LAUNCH_CHECK("build_count_kernel");
         const int64_t ncb = ceil_div(cols, bc);
         int64_t big_blocks = (int64_t)num_sms() * GL_BUILD_COUNT_BIG_CTAS;

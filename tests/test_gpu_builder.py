@@ -121,6 +121,20 @@ def test_builder_hub_stripes_vs_oracle(device):
         assert_pbr_equal(got, want, f"hub b={br} min={mn}")
 
 
+@pytest.mark.parametrize("br,bc,mn", [(6, 10, 2), (12, 5, 3), (16, 4, 4), (32, 2, 2)])
+def test_builder_tall_blocks_vs_oracle(br, bc, mn, device):
+    """Block heights that give a stripe 8, 16 or 32 lanes in the count pass
+    (four, two or one stripe per warp), on the hub graph, so short stripes,
+    long ones and hub stripes all occur."""
+    from page_rank_gb300 import synth
+    g = synth.cluster_rmat_graph(log2n=14, cluster=64, mean_degree=16, p_intra=0.7, seed=6)
+    A = g.A
+    n = A.shape[0]
+    want = oracle.csr_to_pbr(A.indptr, A.indices, A.data, n, A.shape[1], br, bc, mn)
+    _, got = _gpu(A, br, bc, mn)
+    assert_pbr_equal(got, want, f"tall b={br}x{bc} min={mn}")
+
+
 @pytest.mark.parametrize("rows_per_stripe", [2, 8])
 def test_builder_validation_in_long_stripes(rows_per_stripe, device):
     """Out-of-range, unsorted and duplicate columns inside stripes long
@@ -135,7 +149,7 @@ def test_builder_validation_in_long_stripes(rows_per_stripe, device):
     ip = torch.from_numpy(dense.indptr.astype(np.int32)).to(device)
     dv = torch.from_numpy(dense.data).to(device)
     good = dense.indices.astype(np.int32)
-    assert np.diff(dense.indptr).max() * rows_per_stripe > 2048
+    assert np.diff(dense.indptr).max() * rows_per_stripe > 2048   # counted by a CTA
     build_pbr_device(ip, torch.from_numpy(good).to(device), dv, 16, 30000, rows_per_stripe, rows_per_stripe, 1)
     k = int(dense.indptr[3]) + 100           # an entry in the middle of row 3
     bad_range = good.copy()
