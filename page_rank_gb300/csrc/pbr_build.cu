@@ -75,8 +75,13 @@ enum BuildWork {
 };
 constexpr int64_t kHugeEntries = 4096;
 // Stripes with up to this many distinct blocks are ordered by one warp
-// (build_fill_kernel), bigger ones by a CTA (build_fill_big_kernel).
-constexpr int kSmallStripeBlocks = 64;
+// (build_fill_kernel, O(m^2 / 32) comparisons per lane), bigger ones by a
+// CTA (build_fill_big_kernel, O(m) sorts and scans with a fixed cost of a few
+// dozen block-wide barriers).
+#ifndef GL_BUILD_SMALL_BLOCKS
+#define GL_BUILD_SMALL_BLOCKS 64
+#endif
+constexpr int kSmallStripeBlocks = GL_BUILD_SMALL_BLOCKS;
 
 // Workspace layout (every region 256-byte aligned).
 struct BuildWs {
@@ -905,7 +910,7 @@ build_count_big_kernel(const I* indptr, const I* indices, int64_t rows, int64_t 
 // order_stripe for a big stripe (one 1024-thread CTA; see the section
 // comment above).  Same outputs as order_stripe.
 template <typename I>
-__device__ void order_stripe_big(BigShared& sh, int64_t s, int m, int br, int bc, int min_nnz, int64_t ncb,
+__device__ void order_stripe_big(BigShared& sh, int64_t s, int m, int n, int br, int bc, int min_nnz, int64_t ncb,
                                  bool key32, int nchain, const int64_t* chain, int64_t prefmax, int64_t kept_base,
                                  int64_t packed_base, const BigRecs& r, uint64_t* out_codes, I* out_coords,
                                  I* out_offsets) {
@@ -916,7 +921,8 @@ __device__ void order_stripe_big(BigShared& sh, int64_t s, int m, int br, int bc
         r.v0[e] = e;
     }
     __syncthreads();
-    big_sort(sh, r.k0, r.v0, r.k1, r.v1, m, 31);   // by first CSR position
+    // by first CSR position (stripe-local, below n)
+    big_sort(sh, r.k0, r.v0, r.k1, r.v1, m, n > 1 ? 32 - __clz(n - 1) : 1);
     for (int i = t; i < m; i += kBigThreads) r.ins[r.v0[i]] = i;   // insertion rank
     __syncthreads();
     for (int e = t; e < m; e += kBigThreads) r.tau[e] = r.ins[e];
@@ -1074,7 +1080,7 @@ build_fill_big_kernel(const I* indptr, const I* indices, const S* values, int64_
         }
         record_blocks_big<I>(sh, indptr, indices, s, rows, br, bc, ncb, en, const_cast<uint64_t*>(r.code),
                              const_cast<int64_t*>(r.bcol), r.ins);
-        order_stripe_big<I>(sh, s, m, br, bc, min_nnz, ncb, key32, nchain, w.chain, w.stripe_prefmax[s],
+        order_stripe_big<I>(sh, s, m, (int)n, br, bc, min_nnz, ncb, key32, nchain, w.chain, w.stripe_prefmax[s],
                             w.stripe_kept[s], w.stripe_packed[s], r, out_codes, out_coords, out_offsets);
         move_values_big<I, S>(sh, indptr, indices, values, s, rows, br, en, r.tau, r.g,
                               w.stripe_packed[s], w.row_rem, out_data, out_rem_col, out_rem_val);
