@@ -155,7 +155,8 @@ int64_t gl_pbr_build_workspace_bytes(int64_t rows, int64_t cols, int64_t nnz,
  * scans them.  Synchronizes `stream` to return the totals in *counts.
  * index_type: GL_I32 or GL_I64 for indptr and indices.
  * Errors: GL_ERR_INVALID_ARGUMENT (block_rows * block_cols > 64, an index out
- * of range, min_nnz outside 0..255), GL_ERR_NONCANONICAL, GL_ERR_WORKSPACE. */
+ * of range, min_nnz outside 0..255, 2^30 or more stripes),
+ * GL_ERR_NONCANONICAL, GL_ERR_WORKSPACE. */
 int gl_pbr_build_count(const void* indptr, const void* indices, int32_t index_type,
                        int64_t rows, int64_t cols, int64_t nnz,
                        int32_t block_rows, int32_t block_cols, int32_t min_nnz_per_block,
@@ -166,7 +167,9 @@ int gl_pbr_build_count(const void* indptr, const void* indices, int32_t index_ty
  * reference's PBRMatrixInt32* / PBRMatrixInt64* variants), values use
  * value_type.  block_codes receives the raw 64-bit masks.  stripe_block_ptr
  * (int32, ceil(rows/block_rows)+1 entries) may be NULL.  Must follow
- * gl_pbr_build_count with the same arguments and workspace. */
+ * gl_pbr_build_count with the same arguments and workspace; it may be
+ * repeated after one count (it resets the counters its kernels draw stripes
+ * from).  Synchronizes `stream`. */
 int gl_pbr_build_fill(const void* indptr, const void* indices, const void* values,
                       int32_t index_type, int32_t value_type,
                       int64_t rows, int64_t cols, int64_t nnz,

@@ -168,3 +168,46 @@ def test_builder_validation_in_long_stripes(rows_per_stripe, device):
             build_pbr_device(ip, torch.from_numpy(arr).to(device), dv, 16, 30000, rows_per_stripe,
                              rows_per_stripe, 1)
         assert ei.value.code == native.GL_ERR_NONCANONICAL
+
+
+def test_fill_repeated_after_one_count(device):
+    """gl_pbr_build_fill run twice after one gl_pbr_build_count on the same
+    workspace writes the same arrays both times: the fill resets the
+    counters its kernels draw stripes from (short stripes, long ones in
+    shared and in global scratch)."""
+    import torch
+
+    from page_rank_gb300 import native, synth
+    from page_rank_gb300.pbr import _stream_handle
+    g = synth.cluster_rmat_graph(log2n=13, cluster=64, mean_degree=16, p_intra=0.7, seed=8)
+    A = g.A
+    n, nnz = A.shape[0], A.nnz
+    ip = torch.from_numpy(A.indptr.astype(np.int32)).to(device)
+    ix = torch.from_numpy(A.indices.astype(np.int32)).to(device)
+    dv = torch.from_numpy(A.data.astype(np.float32)).to(device)
+    L = native.lib()
+    ws_bytes = int(L.gl_pbr_build_workspace_bytes(n, n, nnz, 8, 8))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=device)
+    stream = _stream_handle(device)
+    counts = native.BuildCounts()
+    native.check(L.gl_pbr_build_count(ip.data_ptr(), ix.data_ptr(), native.GL_I32, n, n, nnz, 8, 8, 8,
+                                      ws.data_ptr(), ws_bytes, counts, stream))
+    assert counts.max_stripe_blocks > 64
+    want = oracle.csr_to_pbr(A.indptr, A.indices, A.data, n, n, 8, 8, 8)
+    nb, packed, rem = counts.num_blocks, counts.packed_nnz, counts.remainder_nnz
+    for _ in range(2):
+        out = {"block_codes": torch.empty(nb, dtype=torch.int64, device=device),
+               "block_coords": torch.empty(2 * nb, dtype=torch.int32, device=device),
+               "block_offsets": torch.empty(nb + 1, dtype=torch.int32, device=device),
+               "block_data": torch.empty(packed, dtype=torch.float32, device=device),
+               "remainder_indptr": torch.empty(n + 1, dtype=torch.int32, device=device),
+               "remainder_col_ind": torch.empty(rem, dtype=torch.int32, device=device),
+               "remainder_data": torch.empty(rem, dtype=torch.float32, device=device)}
+        sp_ptr = torch.empty(-(-n // 8) + 1, dtype=torch.int32, device=device)
+        native.check(L.gl_pbr_build_fill(
+            ip.data_ptr(), ix.data_ptr(), dv.data_ptr(), native.GL_I32, native.GL_F32, n, n, nnz, 8, 8, 8,
+            ws.data_ptr(), ws_bytes, counts, *(out[k].data_ptr() for k in PBR_KEYS), sp_ptr.data_ptr(), stream))
+        torch.cuda.synchronize(device)
+        got = {k: v.cpu().numpy() for k, v in out.items()}
+        got["block_codes"] = got["block_codes"].view(np.uint64)
+        assert_pbr_equal(got, want, "repeated fill")
