@@ -408,12 +408,11 @@ __device__ __forceinline__ uint32_t key_bucket(int64_t key_value, bool key32, ui
 // A team is the set of threads that orders one stripe with order_stripe: a
 // warp, for stripes with up to kSmallStripeBlocks distinct blocks (bigger
 // ones go through order_stripe_big).
+// A warp holds 32 / TEAM teams, each ordering its own stripe.
 template <int TEAM>
-struct Team;
-template <>
-struct Team<32> {
-    static __device__ __forceinline__ int rank() { return threadIdx.x & 31; }
-    static __device__ __forceinline__ void sync() { __syncwarp(); }
+struct Team {
+    static __device__ __forceinline__ int rank() { return threadIdx.x & (TEAM - 1); }
+    static __device__ __forceinline__ void sync() { __syncwarp(group_mask<TEAM>()); }
 };
 
 constexpr int kBigThreads = 1024;
@@ -452,14 +451,14 @@ __device__ void list_order(int64_t s, int64_t ncb, bool key32, uint64_t buckets,
     Team<TEAM>::sync();
 }
 
-// Records the distinct blocks of stripe s in block-column order (warp 0 of
-// the team): code, block column and first CSR position relative to the
+// Records the distinct blocks of stripe s in block-column order (a group of
+// G lanes): code, block column and first CSR position relative to the
 // stripe start.
-template <typename I>
+template <typename I, int G>
 __device__ void record_blocks(const I* indptr, const I* indices, int64_t s, int64_t rows, int64_t cols, int64_t nnz,
                               int br, int bc, uint64_t* code_r, int64_t* bcol_r, int32_t* first_r) {
-    const int lane = threadIdx.x & 31;
-    StripeMerge<I> mg;
+    const int lane = threadIdx.x & (G - 1);
+    StripeMerge<I, G> mg;
     mg.init(indptr, indices, s, rows, nnz, br, bc, false);
     int64_t bcol, first, my_first;
     uint64_t code;
@@ -476,15 +475,17 @@ __device__ void record_blocks(const I* indptr, const I* indices, int64_t s, int6
     }
 }
 
-// Moves the stripe's values into block_data / the remainder (warp 0):
-// slot[j] >= 0 is the output slot of kept block j, doff[j] its value offset.
-template <typename I, typename S>
+// Moves the stripe's values into block_data / the remainder (a group of G
+// lanes): slot[j] >= 0 is the output slot of kept block j, doff[j] its value
+// offset.
+template <typename I, typename S, int G>
 __device__ void move_values(const I* indptr, const I* indices, const S* values, int64_t s, int64_t rows,
                             int64_t cols, int64_t nnz, int br, int bc, const int32_t* slot, const int32_t* doff,
                             int64_t packed_base, const int64_t* row_rem, S* out_data, I* out_rem_col,
                             S* out_rem_val) {
-    const int lane = threadIdx.x & 31;
-    StripeMerge<I> mg;
+    const int lane = threadIdx.x & (G - 1);
+    const unsigned gmask = group_mask<G>();
+    StripeMerge<I, G> mg;
     mg.init(indptr, indices, s, rows, nnz, br, bc, false);
     const int64_t row = s * br + lane;
     int64_t rem_cursor = (lane < br && row < rows) ? row_rem[row] : 0;
@@ -494,7 +495,13 @@ __device__ void move_values(const I* indptr, const I* indices, const S* values, 
     int j = 0;
     while (mg.template step<false>(cols, bcol, code, first, my_count, my_first)) {
         if (slot[j] >= 0) {
-            const int before = (int)warp_incl_scan_i64(my_count) - my_count;
+            int incl = my_count;   // inclusive scan over the group's rows
+#pragma unroll
+            for (int o = 1; o < G; o <<= 1) {
+                const int u = __shfl_up_sync(gmask, incl, o, G);
+                if (lane >= o) incl += u;
+            }
+            const int before = incl - my_count;
             const int64_t dst = packed_base + doff[j] + before;
             for (int i = 0; i < my_count; ++i) out_data[dst + i] = values[my_first + i];
         } else {
@@ -1022,29 +1029,30 @@ __device__ void order_stripe(int64_t s, int m, int br, int bc, int min_nnz, int6
     Team<TEAM>::sync();
 }
 
-template <typename I, typename S>
+// G lanes per stripe (block_rows <= G), 32 / G stripes per warp at a time.
+template <typename I, typename S, int G>
 __global__ void __launch_bounds__(kBuildThreads)
 build_fill_kernel(const I* indptr, const I* indices, const S* values, int64_t rows, int64_t cols, int64_t nnz,
                   int br, int bc, int min_nnz, int64_t nstripes, int64_t ncb, bool key32, int nchain,
                   BuildWs w, uint64_t* out_codes, I* out_coords, I* out_offsets, S* out_data,
                   I* out_rem_col, S* out_rem_val, int32_t* out_stripe_ptr) {
-    const int lane = threadIdx.x & 31;
-    for (WarpDraw d(&w.work[kWorkFillWarpDraw], nstripes); d.next();) {
+    const int lane = threadIdx.x & (G - 1);
+    for (WarpDraw<G> d(&w.work[kWorkFillWarpDraw], nstripes); d.next();) {
         const int64_t s = d.s;
         const int64_t rbase = w.stripe_m[s];
         const int m = (int)(w.stripe_m[s + 1] - rbase);
         const int64_t kept_base = w.stripe_kept[s];
         if (lane == 0 && out_stripe_ptr) out_stripe_ptr[s] = (int32_t)kept_base;
         if (m == 0 || m > kSmallStripeBlocks) continue;   // big stripes: build_fill_big_kernel
-        record_blocks<I>(indptr, indices, s, rows, cols, nnz, br, bc, w.rec_code + rbase, w.rec_bcol + rbase,
-                         w.rec_ins + rbase);
-        __syncwarp();
-        order_stripe<32, I>(s, m, br, bc, min_nnz, ncb, key32, nchain, w.chain, w.stripe_prefmax[s], kept_base,
+        record_blocks<I, G>(indptr, indices, s, rows, cols, nnz, br, bc, w.rec_code + rbase, w.rec_bcol + rbase,
+                            w.rec_ins + rbase);
+        __syncwarp(group_mask<G>());
+        order_stripe<G, I>(s, m, br, bc, min_nnz, ncb, key32, nchain, w.chain, w.stripe_prefmax[s], kept_base,
                             w.stripe_packed[s], w.rec_code + rbase, w.rec_bcol + rbase, w.rec_ins + rbase,
                             w.rec_tau + rbase, w.rec_bkt + rbase, w.rec_g + rbase, w.rec_pos + rbase,
                             w.rec_pops + rbase, out_codes, out_coords, out_offsets);
-        move_values<I, S>(indptr, indices, values, s, rows, cols, nnz, br, bc, w.rec_tau + rbase, w.rec_g + rbase,
-                          w.stripe_packed[s], w.row_rem, out_data, out_rem_col, out_rem_val);
+        move_values<I, S, G>(indptr, indices, values, s, rows, cols, nnz, br, bc, w.rec_tau + rbase,
+                             w.rec_g + rbase, w.stripe_packed[s], w.row_rem, out_data, out_rem_col, out_rem_val);
     }
 }
 
@@ -1275,9 +1283,17 @@ int fill_impl(const I* indptr, const I* indices, const S* values, int64_t rows, 
         int64_t blocks = ceil_div(ns, kBuildWarps);
         const int64_t cap = (int64_t)num_sms() * 16;
         if (blocks > cap) blocks = cap;
-        build_fill_kernel<I, S><<<(unsigned)blocks, kBuildThreads, 0, stream>>>(
-            indptr, indices, values, rows, cols, nnz, br, bc, min_nnz, ns, (int64_t)ncb, sizeof(I) == 4, nchain, w, codes,
-            coords, offsets, data, rem_col, rem_val, stripe_ptr);
+#ifndef GL_BUILD_FILL_GROUP
+#define GL_BUILD_FILL_GROUP 8
+#endif
+#define GL_FILL_LAUNCH(G)                                                                                        \
+    build_fill_kernel<I, S, G><<<(unsigned)blocks, kBuildThreads, 0, stream>>>(                                   \
+        indptr, indices, values, rows, cols, nnz, br, bc, min_nnz, ns, (int64_t)ncb, sizeof(I) == 4, nchain, w,   \
+        codes, coords, offsets, data, rem_col, rem_val, stripe_ptr)
+        if (br <= 8 && GL_BUILD_FILL_GROUP <= 8) GL_FILL_LAUNCH(8);
+        else if (br <= 16 && GL_BUILD_FILL_GROUP <= 16) GL_FILL_LAUNCH(16);
+        else GL_FILL_LAUNCH(32);
+#undef GL_FILL_LAUNCH
         GL_LAUNCH_CHECK("build_fill_kernel");
         if (counts->max_stripe_blocks > kSmallStripeBlocks) {
             int64_t big_blocks = (int64_t)num_sms() * GL_BUILD_FILL_BIG_CTAS;
