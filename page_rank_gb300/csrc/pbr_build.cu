@@ -282,6 +282,11 @@ constexpr int kSmemEntries = GL_BUILD_SMEM_ENTRIES;
 // launched with): the count kernel keeps 64 registers (at 32 it spills and
 // was 6 % slower), the fill kernel runs two CTAs per SM on 1024-entry shared
 // scratch (faster than one CTA on 1536 or 2048 entries).
+// The CTA kernels' radix-sort and scan tiles load the next tile's elements
+// before working on the current one (0: after).
+#ifndef GL_BUILD_SORT_PREFETCH
+#define GL_BUILD_SORT_PREFETCH 1
+#endif
 #ifndef GL_BUILD_COUNT_BIG_CTAS
 #define GL_BUILD_COUNT_BIG_CTAS 1
 #endif
@@ -563,9 +568,13 @@ __device__ void big_scan(BigShared& sh, int32_t* a, int n, bool inclusive) {
     auto op = [](int32_t x, int32_t y) { return MAX ? (x > y ? x : y) : x + y; };
     if (t == 0) sh.carry = ident;
     __syncthreads();
+    // Each tile's element is loaded one tile ahead (a[] may be global
+    // scratch; the scan writes only the current tile).
+    int32_t x_next = t < n ? a[t] : ident;
     for (int base = 0; base < n; base += kBigThreads) {
         const int i = base + t;
-        const int32_t x = i < n ? a[i] : ident;
+        const int32_t x = x_next;
+        if (GL_BUILD_SORT_PREFETCH) x_next = i + kBigThreads < n ? a[i + kBigThreads] : ident;
         int32_t v = x;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -587,6 +596,7 @@ __device__ void big_scan(BigShared& sh, int32_t* a, int n, bool inclusive) {
         const int32_t c = sh.carry;
         const int32_t incl = op(c, warp > 0 ? op(sh.warp_tot[warp - 1], v) : v);
         if (i < n) a[i] = (inclusive || MAX) ? incl : incl - x;
+        if (!GL_BUILD_SORT_PREFETCH) x_next = i + kBigThreads < n ? a[i + kBigThreads] : ident;
         __syncthreads();
         if (t == 0) sh.carry = op(c, sh.warp_tot[kBigThreads / 32 - 1]);
         __syncthreads();
@@ -626,11 +636,26 @@ __device__ void big_sort(BigShared& sh, int32_t* k, int32_t* v, int32_t* kt, int
             }
         }
         __syncthreads();
+        // the next tile's pair is loaded while this one is ranked (sources
+        // and destinations are different arrays)
+        int32_t key_next = 0, val_next = 0;
+        if (GL_BUILD_SORT_PREFETCH && t < n) {
+            key_next = ks[t];
+            val_next = vs[t];
+        }
         for (int base = 0; base < n; base += kBigThreads) {   // tiles in order: stable
             const int i = base + t;
             const bool ok = i < n;
-            const int32_t key = ok ? ks[i] : 0;
-            const int32_t val = ok ? vs[i] : 0;
+            int32_t key, val;
+            if (GL_BUILD_SORT_PREFETCH) {
+                key = key_next;
+                val = val_next;
+                key_next = i + kBigThreads < n ? ks[i + kBigThreads] : 0;
+                val_next = i + kBigThreads < n ? vs[i + kBigThreads] : 0;
+            } else {
+                key = ok ? ks[i] : 0;
+                val = ok ? vs[i] : 0;
+            }
             const int d = ok ? (int)(((uint32_t)key >> shift) & 255u) : 256;
             for (int q = lane; q < 256; q += 32) sh.wcnt[warp][q] = 0;
             __syncwarp();
