@@ -287,6 +287,12 @@ constexpr int kSmemEntries = GL_BUILD_SMEM_ENTRIES;
 #ifndef GL_BUILD_SORT_PREFETCH
 #define GL_BUILD_SORT_PREFETCH 1
 #endif
+// Unroll factor of the CTA kernels' element loops (2 and 4 spilled in the
+// fill kernel's 32 registers and were 2-6 % slower than 1).
+#ifndef GL_BUILD_UNROLL
+#define GL_BUILD_UNROLL 1
+#endif
+constexpr int kUnroll = GL_BUILD_UNROLL;
 #ifndef GL_BUILD_COUNT_BIG_CTAS
 #define GL_BUILD_COUNT_BIG_CTAS 1
 #endif
@@ -619,7 +625,18 @@ __device__ void big_sort(BigShared& sh, int32_t* k, int32_t* v, int32_t* kt, int
         int32_t* vd = (pass & 1) ? v : vt;
         if (t < 256) sh.hist[t] = 0;
         __syncthreads();
-        for (int i = t; i < n; i += kBigThreads) atomicAdd(&sh.hist[((uint32_t)ks[i] >> shift) & 255u], 1);
+        {   // four keys in flight per thread (ks may be global scratch)
+            int i = t;
+            for (; i + 3 * kBigThreads < n; i += 4 * kBigThreads) {
+                const uint32_t a0 = (uint32_t)ks[i], a1 = (uint32_t)ks[i + kBigThreads];
+                const uint32_t a2 = (uint32_t)ks[i + 2 * kBigThreads], a3 = (uint32_t)ks[i + 3 * kBigThreads];
+                atomicAdd(&sh.hist[(a0 >> shift) & 255u], 1);
+                atomicAdd(&sh.hist[(a1 >> shift) & 255u], 1);
+                atomicAdd(&sh.hist[(a2 >> shift) & 255u], 1);
+                atomicAdd(&sh.hist[(a3 >> shift) & 255u], 1);
+            }
+            for (; i < n; i += kBigThreads) atomicAdd(&sh.hist[((uint32_t)ks[i] >> shift) & 255u], 1);
+        }
         __syncthreads();
         if (warp == 0) {   // exclusive scan of the histogram: digit bases
             int32_t run = 0;
@@ -691,44 +708,66 @@ __device__ void big_sort(BigShared& sh, int32_t* k, int32_t* v, int32_t* kt, int
 __device__ void list_order_big(BigShared& sh, int64_t s, int64_t ncb, bool key32, uint64_t buckets, int m,
                                int present, const BigRecs& r) {
     const int t = threadIdx.x;
+    // The record arrays are distinct, and below they are reached only through
+    // these pointers (and pointers passed on from them); saying so lets the
+    // compiler keep several iterations' loads in flight (huge stripes keep
+    // them in global memory, where each round trip costs hundreds of cycles).
+    const int64_t* __restrict__ bcol = r.bcol;
+    const int32_t* __restrict__ ins = r.ins;
+    const int32_t* __restrict__ tau = r.tau;
+    uint32_t* __restrict__ bkt = r.bkt;
+    int32_t* __restrict__ g = r.g;
+    int32_t* __restrict__ pos = r.pos;
+    int32_t* __restrict__ k0 = r.k0;
+    int32_t* __restrict__ v0 = r.v0;
+    int32_t* __restrict__ k1 = r.k1;
+    int32_t* __restrict__ v1 = r.v1;
+#pragma unroll kUnroll
     for (int e = t; e < m; e += kBigThreads) {
-        if (r.ins[e] >= present) continue;
-        const uint32_t b = key_bucket(s * ncb + r.bcol[e], key32, buckets);
-        r.bkt[e] = b;
-        r.v0[r.tau[e]] = e;   // records in rank order
+        if (ins[e] >= present) continue;
+        const uint32_t b = key_bucket(s * ncb + bcol[e], key32, buckets);
+        bkt[e] = b;
+        v0[tau[e]] = e;   // records in rank order
     }
     __syncthreads();
-    for (int i = t; i < present; i += kBigThreads) r.k0[i] = (int32_t)r.bkt[r.v0[i]];
+#pragma unroll kUnroll
+    for (int i = t; i < present; i += kBigThreads) k0[i] = (int32_t)bkt[v0[i]];
     __syncthreads();
     const int bits = buckets > 1 ? 64 - __clzll((long long)(buckets - 1)) : 1;
-    big_sort(sh, r.k0, r.v0, r.k1, r.v1, present, bits);   // bucket runs, each in rank order
-    for (int i = t; i < present; i += kBigThreads) r.k1[i] = (i == 0 || r.k0[i] != r.k0[i - 1]) ? i : -1;
+    big_sort(sh, k0, v0, k1, v1, present, bits);   // bucket runs, each in rank order
+#pragma unroll kUnroll
+    for (int i = t; i < present; i += kBigThreads) k1[i] = (i == 0 || k0[i] != k0[i - 1]) ? i : -1;
     __syncthreads();
-    big_scan<true>(sh, r.k1, present, true);   // k1[i] = first sorted index of i's run
+    big_scan<true>(sh, k1, present, true);   // k1[i] = first sorted index of i's run
+#pragma unroll kUnroll
     for (int i = t; i < present; i += kBigThreads) {
-        const bool last = (i + 1 == present) || (r.k0[i + 1] != r.k0[i]);
-        if (last) r.v1[r.k1[i]] = i - r.k1[i] + 1;   // run length, at the run start
+        const bool last = (i + 1 == present) || (k0[i + 1] != k0[i]);
+        if (last) v1[k1[i]] = i - k1[i] + 1;   // run length, at the run start
     }
     __syncthreads();
     // head rank of each record's run, and its later run-mates
+#pragma unroll kUnroll
     for (int i = t; i < present; i += kBigThreads) {
-        const int e = r.v0[i];
-        const int st = r.k1[i];
-        r.g[e] = r.tau[r.v0[st]];
-        r.pos[e] = r.v1[st] - 1 - (i - st);
+        const int e = v0[i];
+        const int st = k1[i];
+        g[e] = tau[v0[st]];
+        pos[e] = v1[st] - 1 - (i - st);
     }
     __syncthreads();
     // run sizes indexed by head rank, inclusive prefix: records in runs whose
     // head is at most h; the runs with later heads come first in the list
-    for (int h = t; h < present; h += kBigThreads) r.k0[h] = 0;
+#pragma unroll kUnroll
+    for (int h = t; h < present; h += kBigThreads) k0[h] = 0;
     __syncthreads();
+#pragma unroll kUnroll
     for (int i = t; i < present; i += kBigThreads)
-        if (r.k1[i] == i) r.k0[r.tau[r.v0[i]]] = r.v1[i];
+        if (k1[i] == i) k0[tau[v0[i]]] = v1[i];
     __syncthreads();
-    big_scan<false>(sh, r.k0, present, true);
+    big_scan<false>(sh, k0, present, true);
     const int32_t total = present;
+#pragma unroll kUnroll
     for (int e = t; e < m; e += kBigThreads)
-        if (r.ins[e] < present) r.pos[e] += total - r.k0[r.g[e]];
+        if (ins[e] < present) pos[e] += total - k0[g[e]];
     __syncthreads();
 }
 
@@ -768,31 +807,58 @@ __device__ void record_blocks_big(BigShared& sh, const I* indptr, const I* indic
     const int64_t e0 = (int64_t)indptr[r0];
     const int n = (int)((int64_t)indptr[r1] - e0);
     if (t <= br) sh.rowstart[t] = (int32_t)((int64_t)indptr[r0 + t < r1 ? r0 + t : r1] - e0);
-    for (int i = t; i < n; i += kBigThreads) {
-        en.a[i] = (int32_t)((int64_t)indices[e0 + i] / bc);
-        en.b[i] = i;
+    {   // (restrict pointers scoped to each loop: the arrays are distinct)
+        const I* __restrict__ idx = indices + e0;
+        int32_t* __restrict__ a = en.a;
+        int32_t* __restrict__ b = en.b;
+#pragma unroll kUnroll
+        for (int i = t; i < n; i += kBigThreads) {
+            a[i] = (int32_t)((int64_t)idx[i] / bc);
+            b[i] = i;
+        }
     }
     __syncthreads();
     const int bits = 64 - __clzll((long long)(ncb > 1 ? ncb - 1 : 1));
     big_sort(sh, en.a, en.b, en.c, en.d, n, bits);
-    for (int p = t; p < n; p += kBigThreads) en.c[p] = (p == 0 || en.a[p] != en.a[p - 1]) ? 1 : 0;
+    {
+        const int32_t* __restrict__ a = en.a;
+        int32_t* __restrict__ c = en.c;
+#pragma unroll kUnroll
+        for (int p = t; p < n; p += kBigThreads) c[p] = (p == 0 || a[p] != a[p - 1]) ? 1 : 0;
+    }
     __syncthreads();
     big_scan<false>(sh, en.c, n, true);   // run index + 1
-    for (int p = t; p < n; p += kBigThreads) {
-        if (p == 0 || en.a[p] != en.a[p - 1]) {
-            const int j = en.c[p] - 1;
-            en.d[j] = p;
-            bcol_r[j] = en.a[p];
-            first_r[j] = en.b[p];
-            code_r[j] = 0;
+    {
+        const int32_t* __restrict__ a = en.a;
+        const int32_t* __restrict__ b = en.b;
+        const int32_t* __restrict__ c = en.c;
+        int32_t* __restrict__ d = en.d;
+        int64_t* __restrict__ bcol = bcol_r;
+        int32_t* __restrict__ first = first_r;
+        uint64_t* __restrict__ code = code_r;
+#pragma unroll kUnroll
+        for (int p = t; p < n; p += kBigThreads) {
+            if (p == 0 || a[p] != a[p - 1]) {
+                const int j = c[p] - 1;
+                d[j] = p;
+                bcol[j] = a[p];
+                first[j] = b[p];
+                code[j] = 0;
+            }
         }
     }
     __syncthreads();
-    for (int p = t; p < n; p += kBigThreads) {
-        const int i = en.b[p];
-        const int r = big_row_of(sh, br, i);
-        const int64_t col = (int64_t)indices[e0 + i];
-        atomicOr(reinterpret_cast<unsigned long long*>(code_r + (en.c[p] - 1)), 1ull << (r * bc + (int)(col % bc)));
+    {
+        const I* __restrict__ idx = indices + e0;
+        const int32_t* __restrict__ b = en.b;
+        const int32_t* __restrict__ c = en.c;
+#pragma unroll kUnroll
+        for (int p = t; p < n; p += kBigThreads) {
+            const int i = b[p];
+            const int r = big_row_of(sh, br, i);
+            const int64_t col = (int64_t)idx[i];
+            atomicOr(reinterpret_cast<unsigned long long*>(code_r + (c[p] - 1)), 1ull << (r * bc + (int)(col % bc)));
+        }
     }
     __syncthreads();
 }
@@ -812,24 +878,43 @@ __device__ void move_values_big(BigShared& sh, const I* indptr, const I* indices
     const int64_t r1 = r0 + br < rows ? r0 + br : rows;
     const int64_t e0 = (int64_t)indptr[r0];
     const int n = (int)((int64_t)indptr[r1] - e0);
-    for (int p = t; p < n; p += kBigThreads) {
-        const int j = en.c[p] - 1;
-        const int i = en.b[p];
-        const int sl = slot[j];
-        if (sl >= 0) out_data[packed_base + doff[j] + (p - en.d[j])] = values[e0 + i];
-        en.a[i] = sl < 0 ? 1 : 0;
+    {   // (restrict pointers scoped to each loop: the arrays are distinct)
+        const int32_t* __restrict__ b = en.b;
+        const int32_t* __restrict__ c = en.c;
+        const int32_t* __restrict__ d = en.d;
+        const int32_t* __restrict__ sl_r = slot;
+        const int32_t* __restrict__ doff_r = doff;
+        const S* __restrict__ val = values + e0;
+        S* __restrict__ out = out_data + packed_base;
+        int32_t* __restrict__ a = en.a;
+#pragma unroll kUnroll
+        for (int p = t; p < n; p += kBigThreads) {
+            const int j = c[p] - 1;
+            const int i = b[p];
+            const int sl = sl_r[j];
+            if (sl >= 0) out[doff_r[j] + (p - d[j])] = val[i];
+            a[i] = sl < 0 ? 1 : 0;
+        }
     }
     __syncthreads();
     big_scan<false>(sh, en.a, n, true);
-    for (int i = t; i < n; i += kBigThreads) {
-        const int32_t before = i > 0 ? en.a[i - 1] : 0;
-        if (en.a[i] == before) continue;   // kept
-        const int r = big_row_of(sh, br, i);
-        const int rs = sh.rowstart[r];
-        const int32_t row_before = rs > 0 ? en.a[rs - 1] : 0;
-        const int64_t dst = row_rem[r0 + r] + (before - row_before);
-        out_rem_col[dst] = indices[e0 + i];
-        out_rem_val[dst] = values[e0 + i];
+    {
+        const int32_t* __restrict__ a = en.a;
+        const I* __restrict__ idx = indices + e0;
+        const S* __restrict__ val = values + e0;
+        I* __restrict__ rcol = out_rem_col;
+        S* __restrict__ rval = out_rem_val;
+#pragma unroll kUnroll
+        for (int i = t; i < n; i += kBigThreads) {
+            const int32_t before = i > 0 ? a[i - 1] : 0;
+            if (a[i] == before) continue;   // kept
+            const int r = big_row_of(sh, br, i);
+            const int rs = sh.rowstart[r];
+            const int32_t row_before = rs > 0 ? a[rs - 1] : 0;
+            const int64_t dst = row_rem[r0 + r] + (before - row_before);
+            rcol[dst] = idx[i];
+            rval[dst] = val[i];
+        }
     }
     __syncthreads();
 }
@@ -947,52 +1032,97 @@ __device__ void order_stripe_big(BigShared& sh, int64_t s, int m, int n, int br,
                                  int64_t packed_base, const BigRecs& r, uint64_t* out_codes, I* out_coords,
                                  I* out_offsets) {
     const int t = threadIdx.x;
-    for (int e = t; e < m; e += kBigThreads) {
-        r.pops[e] = __popcll(r.code[e]);
-        r.k0[e] = r.ins[e];
-        r.v0[e] = e;
+    // Each loop names the distinct record arrays it touches with restrict
+    // pointers (scoped to the loop, as list_order_big reaches the same arrays
+    // through r), so the compiler keeps several iterations' loads in flight.
+    {
+        const uint64_t* __restrict__ code = r.code;
+        const int32_t* __restrict__ ins = r.ins;
+        int32_t* __restrict__ pops = r.pops;
+        int32_t* __restrict__ k0 = r.k0;
+        int32_t* __restrict__ v0 = r.v0;
+#pragma unroll kUnroll
+        for (int e = t; e < m; e += kBigThreads) {
+            pops[e] = __popcll(code[e]);
+            k0[e] = ins[e];
+            v0[e] = e;
+        }
     }
     __syncthreads();
     // by first CSR position (stripe-local, below n)
     big_sort(sh, r.k0, r.v0, r.k1, r.v1, m, n > 1 ? 32 - __clz(n - 1) : 1);
-    for (int i = t; i < m; i += kBigThreads) r.ins[r.v0[i]] = i;   // insertion rank
+    {
+        int32_t* __restrict__ ins = r.ins;
+        const int32_t* __restrict__ v0 = r.v0;
+#pragma unroll kUnroll
+        for (int i = t; i < m; i += kBigThreads) ins[v0[i]] = i;   // insertion rank
+    }
     __syncthreads();
-    for (int e = t; e < m; e += kBigThreads) r.tau[e] = r.ins[e];
+    {
+        const int32_t* __restrict__ ins = r.ins;
+        int32_t* __restrict__ tau = r.tau;
+#pragma unroll kUnroll
+        for (int e = t; e < m; e += kBigThreads) tau[e] = ins[e];
+    }
     __syncthreads();
     int J = 0;
     while (J + 1 < nchain && chain[2 * (J + 1)] <= prefmax) ++J;
     while (J + 1 < nchain && chain[2 * (J + 1)] <= m) {
         const int present = (int)(chain[2 * (J + 1)] - 1);
         list_order_big(sh, s, ncb, key32, (uint64_t)chain[2 * J + 1], m, present, r);
-        for (int e = t; e < m; e += kBigThreads)
-            if (r.ins[e] < present) r.tau[e] = r.pos[e];
+        {
+            const int32_t* __restrict__ ins = r.ins;
+            const int32_t* __restrict__ pos = r.pos;
+            int32_t* __restrict__ tau = r.tau;
+#pragma unroll kUnroll
+            for (int e = t; e < m; e += kBigThreads)
+                if (ins[e] < present) tau[e] = pos[e];
+        }
         __syncthreads();
         ++J;
     }
     list_order_big(sh, s, ncb, key32, (uint64_t)chain[2 * J + 1], m, m, r);
     // kept flags and popcounts in list order; exclusive scans give slots and
     // value offsets
-    for (int e = t; e < m; e += kBigThreads) {
-        const bool kept = r.pops[e] >= min_nnz;
-        r.k0[r.pos[e]] = kept ? 1 : 0;
-        r.v0[r.pos[e]] = kept ? r.pops[e] : 0;
+    {
+        const int32_t* __restrict__ pops = r.pops;
+        const int32_t* __restrict__ pos = r.pos;
+        int32_t* __restrict__ k0 = r.k0;
+        int32_t* __restrict__ v0 = r.v0;
+#pragma unroll kUnroll
+        for (int e = t; e < m; e += kBigThreads) {
+            const bool kept = pops[e] >= min_nnz;
+            k0[pos[e]] = kept ? 1 : 0;
+            v0[pos[e]] = kept ? pops[e] : 0;
+        }
     }
     __syncthreads();
     big_scan<false>(sh, r.k0, m, false);
     big_scan<false>(sh, r.v0, m, false);
-    for (int e = t; e < m; e += kBigThreads) {
-        int slot = -1, doff = 0;
-        if (r.pops[e] >= min_nnz) {
-            slot = r.k0[r.pos[e]];
-            doff = r.v0[r.pos[e]];
-            const int64_t ob = kept_base + slot;
-            out_codes[ob] = r.code[e];
-            out_coords[2 * ob] = (I)(s * br);
-            out_coords[2 * ob + 1] = (I)(r.bcol[e] * bc);
-            out_offsets[ob] = (I)(packed_base + doff);
+    {
+        const uint64_t* __restrict__ code = r.code;
+        const int64_t* __restrict__ bcol = r.bcol;
+        const int32_t* __restrict__ pops = r.pops;
+        const int32_t* __restrict__ pos = r.pos;
+        const int32_t* __restrict__ k0 = r.k0;
+        const int32_t* __restrict__ v0 = r.v0;
+        int32_t* __restrict__ tau = r.tau;
+        int32_t* __restrict__ g = r.g;
+#pragma unroll kUnroll
+        for (int e = t; e < m; e += kBigThreads) {
+            int slot = -1, doff = 0;
+            if (pops[e] >= min_nnz) {
+                slot = k0[pos[e]];
+                doff = v0[pos[e]];
+                const int64_t ob = kept_base + slot;
+                out_codes[ob] = code[e];
+                out_coords[2 * ob] = (I)(s * br);
+                out_coords[2 * ob + 1] = (I)(bcol[e] * bc);
+                out_offsets[ob] = (I)(packed_base + doff);
+            }
+            tau[e] = slot;
+            g[e] = doff;
         }
-        r.tau[e] = slot;
-        r.g[e] = doff;
     }
     __syncthreads();
 }
