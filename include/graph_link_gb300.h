@@ -152,7 +152,8 @@ int64_t gl_pbr_build_workspace_bytes(int64_t rows, int64_t cols, int64_t nnz,
 
 /* Phase 1: validates the CSR (indices in range, rows strictly increasing),
  * counts blocks / packed values / remainder entries per stripe and row and
- * scans them.  Synchronizes `stream` to return the totals in *counts.
+ * scans them.  Synchronizes `stream` to return the totals in *counts.  Both
+ * phases run on the current device, whose stream `stream` must be.
  * index_type: GL_I32 or GL_I64 for indptr and indices.
  * Errors: GL_ERR_INVALID_ARGUMENT (block_rows * block_cols > 64, an index out
  * of range, min_nnz outside 0..255, 2^30 or more stripes),

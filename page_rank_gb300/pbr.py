@@ -65,8 +65,11 @@ class DeviceBuild:
 def build_pbr_device(indptr: torch.Tensor, indices: torch.Tensor, data: torch.Tensor,
                      rows: int, cols: int, block_rows: int, block_cols: int,
                      min_nnz_per_block: int) -> DeviceBuild:
-    """Build PBR arrays from a canonical device CSR with the GPU builder."""
-    with nvtx_range(f"pbr.build {block_rows}x{block_cols}"):
+    """Build PBR arrays from a canonical device CSR with the GPU builder (with
+    the CSR's device current, whose stream the builder's kernels run on)."""
+    if indptr.device.type != "cuda":
+        raise RuntimeError("build_pbr_device needs CSR tensors in CUDA memory")
+    with torch.cuda.device(indptr.device), nvtx_range(f"pbr.build {block_rows}x{block_cols}"):
         return _build_pbr_device(indptr, indices, data, rows, cols, block_rows, block_cols, min_nnz_per_block)
 
 
