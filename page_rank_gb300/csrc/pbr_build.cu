@@ -1232,7 +1232,9 @@ build_fill_big_kernel(const I* indptr, const I* indices, const S* values, int64_
         BigRecs r{w.rec_code + rbase, w.rec_bcol + rbase, w.rec_ins + rbase, w.rec_tau + rbase,
                   w.rec_bkt + rbase, w.rec_g + rbase, w.rec_pos + rbase, w.rec_pops + rbase,
                   w.rec_k0 + rbase, w.rec_v0 + rbase, w.rec_k1 + rbase, w.rec_v1 + rbase};
-        if (n <= kSmemEntries) {   // m <= n: every block holds an entry
+        // m <= n for a CSR the count pass accepted (every block holds an
+        // entry); anything else stays on the global scratch, sized by nnz
+        if (n >= 0 && n <= kSmemEntries && m <= n) {
             constexpr int K = kSmemEntries;
             uint64_t* d64 = reinterpret_cast<uint64_t*>(build_dyn);
             int32_t* d32 = reinterpret_cast<int32_t*>(d64 + 2 * K);
