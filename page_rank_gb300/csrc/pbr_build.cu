@@ -278,27 +278,30 @@ constexpr int64_t kBigCountEntries = GL_BUILD_BIG_COUNT_ENTRIES;
 #define GL_BUILD_SMEM_ENTRIES 1024
 #endif
 constexpr int kSmemEntries = GL_BUILD_SMEM_ENTRIES;
+
 // Resident 1024-thread CTAs per SM the two CTA kernels are compiled for (and
 // launched with): the count kernel keeps 64 registers (at 32 it spills and
 // was 6 % slower), the fill kernel runs two CTAs per SM on 1024-entry shared
 // scratch (faster than one CTA on 1536 or 2048 entries).
-// The CTA kernels' radix-sort and scan tiles load the next tile's elements
-// before working on the current one (0: after).
-#ifndef GL_BUILD_SORT_PREFETCH
-#define GL_BUILD_SORT_PREFETCH 1
-#endif
-// Unroll factor of the CTA kernels' element loops (2 and 4 spilled in the
-// fill kernel's 32 registers and were 2-6 % slower than 1).
-#ifndef GL_BUILD_UNROLL
-#define GL_BUILD_UNROLL 1
-#endif
-constexpr int kUnroll = GL_BUILD_UNROLL;
 #ifndef GL_BUILD_COUNT_BIG_CTAS
 #define GL_BUILD_COUNT_BIG_CTAS 1
 #endif
 #ifndef GL_BUILD_FILL_BIG_CTAS
 #define GL_BUILD_FILL_BIG_CTAS 2
 #endif
+
+// The CTA kernels' radix-sort and scan tiles load the next tile's elements
+// before working on the current one (0: after).
+#ifndef GL_BUILD_SORT_PREFETCH
+#define GL_BUILD_SORT_PREFETCH 1
+#endif
+
+// Unroll factor of the CTA kernels' element loops (2 and 4 spilled in the
+// fill kernel's 32 registers and were 2-6 % slower than 1).
+#ifndef GL_BUILD_UNROLL
+#define GL_BUILD_UNROLL 1
+#endif
+constexpr int kUnroll = GL_BUILD_UNROLL;
 
 // Hands a warp its stripes: GL_BUILD_WARP_DRAW consecutive stripes per draw
 // from a counter, so warps that drew cheap stripes come back for more (one
