@@ -85,6 +85,13 @@ def test_argument_errors_need_no_gpu():
     assert lib.gl_topk_columns(None, 10, 4, None, 4, native.GL_TOPK_MAX + 1, None, None, None, 0,
                                None) == native.GL_ERR_INVALID_ARGUMENT
     assert lib.gl_topk_columns(None, 10, 4, None, 0, 5, None, None, None, 0, None) == native.GL_OK
+    counts = native.BuildCounts()
+    # 2^30 stripes of 8 rows: beyond the builder's int32 stripe lists
+    assert lib.gl_pbr_build_count(None, None, native.GL_I64, 1 << 33, 1 << 33, 0, 8, 8, 8, None, 0, counts,
+                                  None) == native.GL_ERR_INVALID_ARGUMENT
+    assert "stripes" in lib.gl_last_error().decode()
+    assert lib.gl_pbr_build_count(None, None, native.GL_I32, 16, 16, 0, 9, 9, 1, None, 0, counts,
+                                  None) == native.GL_ERR_INVALID_ARGUMENT   # 81 bits per block
 
 
 def test_descriptor_size_matches_the_library():
