@@ -168,7 +168,8 @@ int gl_pbr_build_count(const void* indptr, const void* indices, int32_t index_ty
  * reference's PBRMatrixInt32* / PBRMatrixInt64* variants), values use
  * value_type.  block_codes receives the raw 64-bit masks.  stripe_block_ptr
  * (int32, ceil(rows/block_rows)+1 entries) may be NULL.  Must follow
- * gl_pbr_build_count with the same arguments and workspace; it may be
+ * gl_pbr_build_count with the same arguments and the workspace as the count
+ * left it (the fill reads the count's per-stripe results there); it may be
  * repeated after one count (it resets the counters its kernels draw stripes
  * from).  Synchronizes `stream`. */
 int gl_pbr_build_fill(const void* indptr, const void* indices, const void* values,

@@ -296,6 +296,19 @@ constexpr int kSmemEntries = GL_BUILD_SMEM_ENTRIES;
 #define GL_BUILD_SORT_PREFETCH 1
 #endif
 
+// Long stripes held in shared scratch are put in block-column order by
+// binary searches in the other rows instead of four radix passes.
+#ifndef GL_BUILD_SMEM_RANK
+#define GL_BUILD_SMEM_RANK 1
+#endif
+
+// The fill pass takes the block-column order of stripes sorted in the
+// workspace by the count pass (their entry indices and run indices) instead
+// of sorting them again.
+#ifndef GL_BUILD_REUSE_COUNT_SORT
+#define GL_BUILD_REUSE_COUNT_SORT 1
+#endif
+
 // Unroll factor of the CTA kernels' element loops (2 and 4 spilled in the
 // fill kernel's 32 registers and were 2-6 % slower than 1).
 #ifndef GL_BUILD_UNROLL
@@ -794,43 +807,124 @@ struct BigEntries {
     int32_t* d;
 };
 
+// Stable block-column order of a stripe whose scratch is in shared memory
+// (n <= kSmemEntries), without the radix passes: the block columns go to c in
+// CSR order, then entry j of row r with block column k has j + (entries of
+// earlier rows with block column <= k) + (entries of later rows with block
+// column < k) entries before it — one binary search per other row in shared
+// memory.  Leaves the block columns in rank order in a and the stripe-local
+// entry indices in b, as the sort does.  b is first filled with the identity
+// and ranks are clamped to [0, n), so rows that are not sorted (input the
+// count pass then rejects) leave every index in range.  Columns are clamped
+// to [0, cols); sh.rowstart holds the row starts.
+template <typename I>
+__device__ void big_rank_smem(const BigShared& sh, const I* indices, int64_t e0, int n, int br, int bc,
+                              int64_t cols, const BigEntries& en) {
+    const int t = threadIdx.x;
+    for (int i = t; i < n; i += kBigThreads) {
+        int64_t col = (int64_t)indices[e0 + i];
+        col = col < 0 ? 0 : (col >= cols ? cols - 1 : col);
+        en.c[i] = (int32_t)(col / bc);
+        en.a[i] = 0;
+        en.b[i] = i;
+    }
+    __syncthreads();
+    int32_t key[kSmemEntries / kBigThreads + 1];
+    int rank[kSmemEntries / kBigThreads + 1];
+#pragma unroll
+    for (int u = 0; u * kBigThreads < kSmemEntries; ++u) {
+        const int i = t + u * kBigThreads;
+        if (i >= n) break;
+        const int r = big_row_of(sh, br, i);
+        const int32_t k = en.c[i];
+        int rk = i - sh.rowstart[r];
+        for (int q = 0; q < br; ++q) {
+            if (q == r) continue;
+            const int q0 = sh.rowstart[q];
+            int lo = q0, hi = sh.rowstart[q + 1];
+            if (q < r) {   // entries with block column <= k
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (en.c[mid] <= k) lo = mid + 1;
+                    else hi = mid;
+                }
+            } else {       // entries with block column < k
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (en.c[mid] < k) lo = mid + 1;
+                    else hi = mid;
+                }
+            }
+            rk += lo > q0 ? lo - q0 : 0;
+        }
+        key[u] = k;
+        rank[u] = rk < 0 ? 0 : (rk >= n ? n - 1 : rk);
+    }
+    __syncthreads();   // c is read by the searches above and written by callers next
+#pragma unroll
+    for (int u = 0; u * kBigThreads < kSmemEntries; ++u) {
+        const int i = t + u * kBigThreads;
+        if (i >= n) break;
+        en.a[rank[u]] = key[u];
+        en.b[rank[u]] = i;
+    }
+    __syncthreads();
+}
+
 // record_blocks for a big stripe, one 1024-thread CTA: the stripe's entries
 // are stable-sorted by block column, so each run of equal block columns is
 // one distinct block with its entries in CSR (= row-major bit) order; the
 // run's first entry is the block's first CSR position.  Leaves the sorted
 // entries, the run index + 1 of each sorted entry (c) and each run's first
 // sorted position (d) for move_values_big.
+// in_smem: the scratch is in shared memory (ranked, not sorted); otherwise
+// it is the workspace, where build_count_big_kernel left this stripe's
+// sorted entry indices (b) and run indices + 1 (c), which are reused.
 template <typename I>
 __device__ void record_blocks_big(BigShared& sh, const I* indptr, const I* indices, int64_t s, int64_t rows,
                                   int br, int bc, int64_t ncb, const BigEntries& en, uint64_t* code_r,
-                                  int64_t* bcol_r, int32_t* first_r) {
+                                  int64_t* bcol_r, int32_t* first_r, bool in_smem) {
     const int t = threadIdx.x;
     const int64_t r0 = s * br;
     const int64_t r1 = r0 + br < rows ? r0 + br : rows;
     const int64_t e0 = (int64_t)indptr[r0];
     const int n = (int)((int64_t)indptr[r1] - e0);
     if (t <= br) sh.rowstart[t] = (int32_t)((int64_t)indptr[r0 + t < r1 ? r0 + t : r1] - e0);
-    {   // (restrict pointers scoped to each loop: the arrays are distinct)
+    if (in_smem && GL_BUILD_SMEM_RANK) {
+        __syncthreads();
+        big_rank_smem<I>(sh, indices, e0, n, br, bc, ncb * bc, en);
+        for (int p = t; p < n; p += kBigThreads) en.c[p] = (p == 0 || en.a[p] != en.a[p - 1]) ? 1 : 0;
+        __syncthreads();
+        big_scan<false>(sh, en.c, n, true);   // run index + 1
+    } else if (!in_smem && GL_BUILD_REUSE_COUNT_SORT) {
         const I* __restrict__ idx = indices + e0;
+        const int32_t* __restrict__ b = en.b;
         int32_t* __restrict__ a = en.a;
-        int32_t* __restrict__ b = en.b;
+        for (int p = t; p < n; p += kBigThreads) a[p] = (int32_t)((int64_t)idx[b[p]] / bc);
+        __syncthreads();
+    } else {
+        {   // (restrict pointers scoped to each loop: the arrays are distinct)
+            const I* __restrict__ idx = indices + e0;
+            int32_t* __restrict__ a = en.a;
+            int32_t* __restrict__ b = en.b;
 #pragma unroll kUnroll
-        for (int i = t; i < n; i += kBigThreads) {
-            a[i] = (int32_t)((int64_t)idx[i] / bc);
-            b[i] = i;
+            for (int i = t; i < n; i += kBigThreads) {
+                a[i] = (int32_t)((int64_t)idx[i] / bc);
+                b[i] = i;
+            }
         }
-    }
-    __syncthreads();
-    const int bits = 64 - __clzll((long long)(ncb > 1 ? ncb - 1 : 1));
-    big_sort(sh, en.a, en.b, en.c, en.d, n, bits);
-    {
-        const int32_t* __restrict__ a = en.a;
-        int32_t* __restrict__ c = en.c;
+        __syncthreads();
+        const int bits = 64 - __clzll((long long)(ncb > 1 ? ncb - 1 : 1));
+        big_sort(sh, en.a, en.b, en.c, en.d, n, bits);
+        {
+            const int32_t* __restrict__ a = en.a;
+            int32_t* __restrict__ c = en.c;
 #pragma unroll kUnroll
-        for (int p = t; p < n; p += kBigThreads) c[p] = (p == 0 || a[p] != a[p - 1]) ? 1 : 0;
+            for (int p = t; p < n; p += kBigThreads) c[p] = (p == 0 || a[p] != a[p - 1]) ? 1 : 0;
+        }
+        __syncthreads();
+        big_scan<false>(sh, en.c, n, true);   // run index + 1
     }
-    __syncthreads();
-    big_scan<false>(sh, en.c, n, true);   // run index + 1
     {
         const int32_t* __restrict__ a = en.a;
         const int32_t* __restrict__ b = en.b;
@@ -968,6 +1062,7 @@ build_count_big_kernel(const I* indptr, const I* indices, int64_t rows, int64_t 
             int32_t* d = reinterpret_cast<int32_t*>(build_dyn);
             en = BigEntries{d, d + kSmemEntries, d + 2 * kSmemEntries, d + 3 * kSmemEntries};
         }
+        const bool in_smem = n <= kSmemEntries;
         for (int i = t; i < n; i += kBigThreads) {
             int64_t col = (int64_t)indices[e0 + i];
             const int r = big_row_of(sh, br, i);
@@ -978,8 +1073,13 @@ build_count_big_kernel(const I* indptr, const I* indices, int64_t rows, int64_t 
             en.b[i] = i;
         }
         __syncthreads();
-        const int bits = 64 - __clzll((long long)(ncb > 1 ? ncb - 1 : 1));
-        big_sort(sh, en.a, en.b, en.c, en.d, n, bits);
+        if (in_smem && GL_BUILD_SMEM_RANK) {
+            big_rank_smem<I>(sh, indices, e0, n, br, bc, cols, en);
+        } else {
+            // (the fill reuses b and c of stripes sorted here in the workspace)
+            const int bits = 64 - __clzll((long long)(ncb > 1 ? ncb - 1 : 1));
+            big_sort(sh, en.a, en.b, en.c, en.d, n, bits);
+        }
         for (int p = t; p < n; p += kBigThreads) en.c[p] = (p == 0 || en.a[p] != en.a[p - 1]) ? 1 : 0;
         __syncthreads();
         big_scan<false>(sh, en.c, n, true);   // run index + 1
@@ -1237,7 +1337,8 @@ build_fill_big_kernel(const I* indptr, const I* indices, const S* values, int64_
                   w.rec_k0 + rbase, w.rec_v0 + rbase, w.rec_k1 + rbase, w.rec_v1 + rbase};
         // m <= n for a CSR the count pass accepted (every block holds an
         // entry); anything else stays on the global scratch, sized by nnz
-        if (n >= 0 && n <= kSmemEntries && m <= n) {
+        const bool in_smem = n >= 0 && n <= kSmemEntries && m <= n;
+        if (in_smem) {
             constexpr int K = kSmemEntries;
             uint64_t* d64 = reinterpret_cast<uint64_t*>(build_dyn);
             int32_t* d32 = reinterpret_cast<int32_t*>(d64 + 2 * K);
@@ -1247,7 +1348,7 @@ build_fill_big_kernel(const I* indptr, const I* indices, const S* values, int64_
                         q + 3 * K, q + 4 * K, q + 5 * K, q + 6 * K, q + 7 * K, q + 8 * K, q + 9 * K};
         }
         record_blocks_big<I>(sh, indptr, indices, s, rows, br, bc, ncb, en, const_cast<uint64_t*>(r.code),
-                             const_cast<int64_t*>(r.bcol), r.ins);
+                             const_cast<int64_t*>(r.bcol), r.ins, in_smem);
         order_stripe_big<I>(sh, s, m, (int)n, br, bc, min_nnz, ncb, key32, nchain, w.chain, w.stripe_prefmax[s],
                             w.stripe_kept[s], w.stripe_packed[s], r, out_codes, out_coords, out_offsets);
         move_values_big<I, S>(sh, indptr, indices, values, s, rows, br, en, r.tau, r.g,
