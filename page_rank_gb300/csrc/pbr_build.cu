@@ -309,6 +309,13 @@ constexpr int kSmemEntries = GL_BUILD_SMEM_ENTRIES;
 #define GL_BUILD_REUSE_COUNT_SORT 1
 #endif
 
+// The warp count keeps the block records of the stripes it merges (code,
+// block column, first position) in the per-entry scratch, and the warp fill
+// copies them instead of merging the stripe's rows once more.
+#ifndef GL_BUILD_REUSE_COUNT_RECORDS
+#define GL_BUILD_REUSE_COUNT_RECORDS 1
+#endif
+
 // Unroll factor of the CTA kernels' element loops (2 and 4 spilled in the
 // fill kernel's 32 registers and were 2-6 % slower than 1).
 #ifndef GL_BUILD_UNROLL
@@ -378,10 +385,13 @@ constexpr int kFillSmemBytes = 16 * kSmemEntries + 56 * kSmemEntries;
 // entries; validation flags.
 // ---------------------------------------------------------------------------
 // G lanes per stripe (block_rows <= G), 32 / G stripes per warp at a time.
+// With `rec` (block columns fit int32), the stripe's block records (code,
+// block column, first position relative to the stripe) are kept in the
+// per-entry scratch at the stripe's CSR range, for build_fill_kernel.
 template <typename I, int G>
 __global__ void __launch_bounds__(kBuildThreads)
 build_count_kernel(const I* indptr, const I* indices, int64_t rows, int64_t cols, int64_t nnz, int br, int bc,
-                   int min_nnz, int64_t nstripes, BuildWs w) {
+                   int min_nnz, int64_t nstripes, BuildWs w, bool rec) {
     const int lane = threadIdx.x & (G - 1);
     const unsigned gmask = group_mask<G>();
     for (WarpDraw<G> d(&w.work[kWorkCountWarpDraw], nstripes); d.next();) {
@@ -398,11 +408,19 @@ build_count_kernel(const I* indptr, const I* indices, int64_t rows, int64_t cols
         uint64_t code;
         int my_count;
         int64_t last_bcol = -1;
-        while (mg.template step<false>(cols, bcol, code, first, my_count, my_first)) {
+        int64_t e0 = (int64_t)indptr[s * br];
+        e0 = e0 < 0 ? 0 : (e0 > nnz ? nnz : e0);
+        while (mg.template step<(GL_BUILD_REUSE_COUNT_RECORDS != 0)>(cols, bcol, code, first, my_count, my_first)) {
             // A negative or out-of-order column makes block columns repeat;
             // the count is still finite and the flags reject the build.
             if (bcol <= last_bcol) mg.bad_order = 1;
             last_bcol = bcol;
+            if (GL_BUILD_REUSE_COUNT_RECORDS && rec && lane == 0 && m < ent) {   // (m < ent: inside the range)
+                w.ent_a[e0 + m] = (int32_t)(uint32_t)code;
+                w.ent_b[e0 + m] = (int32_t)(uint32_t)(code >> 32);
+                w.ent_c[e0 + m] = (int32_t)bcol;
+                w.ent_d[e0 + m] = (int32_t)(first - e0);
+            }
             ++m;
             const int pop = __popcll(code);
             if (pop >= min_nnz) {
@@ -1293,7 +1311,7 @@ __global__ void __launch_bounds__(kBuildThreads)
 build_fill_kernel(const I* indptr, const I* indices, const S* values, int64_t rows, int64_t cols, int64_t nnz,
                   int br, int bc, int min_nnz, int64_t nstripes, int64_t ncb, bool key32, int nchain,
                   BuildWs w, uint64_t* out_codes, I* out_coords, I* out_offsets, S* out_data,
-                  I* out_rem_col, S* out_rem_val, int32_t* out_stripe_ptr) {
+                  I* out_rem_col, S* out_rem_val, int32_t* out_stripe_ptr, bool rec) {
     const int lane = threadIdx.x & (G - 1);
     for (WarpDraw<G> d(&w.work[kWorkFillWarpDraw], nstripes); d.next();) {
         const int64_t s = d.s;
@@ -1302,8 +1320,18 @@ build_fill_kernel(const I* indptr, const I* indices, const S* values, int64_t ro
         const int64_t kept_base = w.stripe_kept[s];
         if (lane == 0 && out_stripe_ptr) out_stripe_ptr[s] = (int32_t)kept_base;
         if (m == 0 || m > kSmallStripeBlocks) continue;   // big stripes: build_fill_big_kernel
-        record_blocks<I, G>(indptr, indices, s, rows, cols, nnz, br, bc, w.rec_code + rbase, w.rec_bcol + rbase,
-                            w.rec_ins + rbase);
+        if (GL_BUILD_REUSE_COUNT_RECORDS && rec && stripe_entries(indptr, s, rows, nnz, br) <= kBigCountEntries) {
+            // the warp count kept this stripe's records
+            const int64_t e0 = (int64_t)indptr[s * br];
+            for (int j = lane; j < m; j += G) {
+                w.rec_code[rbase + j] = (uint64_t)(uint32_t)w.ent_a[e0 + j] | ((uint64_t)(uint32_t)w.ent_b[e0 + j] << 32);
+                w.rec_bcol[rbase + j] = w.ent_c[e0 + j];
+                w.rec_ins[rbase + j] = w.ent_d[e0 + j];
+            }
+        } else {
+            record_blocks<I, G>(indptr, indices, s, rows, cols, nnz, br, bc, w.rec_code + rbase, w.rec_bcol + rbase,
+                                w.rec_ins + rbase);
+        }
         __syncwarp(group_mask<G>());
         order_stripe<G, I>(s, m, br, bc, min_nnz, ncb, key32, nchain, w.chain, w.stripe_prefmax[s], kept_base,
                             w.stripe_packed[s], w.rec_code + rbase, w.rec_bcol + rbase, w.rec_ins + rbase,
@@ -1454,15 +1482,16 @@ int count_impl(const I* indptr, const I* indices, int64_t rows, int64_t cols, in
 #ifndef GL_BUILD_COUNT_GROUP
 #define GL_BUILD_COUNT_GROUP 8
 #endif
+        const bool rec = ceil_div(cols, bc) < (int64_t)INT32_MAX;   // block columns fit the int32 records
         if (br <= 8 && GL_BUILD_COUNT_GROUP <= 8)
             build_count_kernel<I, 8><<<(unsigned)blocks, kBuildThreads, 0, stream>>>(indptr, indices, rows, cols, nnz,
-                                                                                     br, bc, min_nnz, ns, w);
+                                                                                     br, bc, min_nnz, ns, w, rec);
         else if (br <= 16 && GL_BUILD_COUNT_GROUP <= 16)
             build_count_kernel<I, 16><<<(unsigned)blocks, kBuildThreads, 0, stream>>>(indptr, indices, rows, cols,
-                                                                                      nnz, br, bc, min_nnz, ns, w);
+                                                                                      nnz, br, bc, min_nnz, ns, w, rec);
         else
             build_count_kernel<I, 32><<<(unsigned)blocks, kBuildThreads, 0, stream>>>(indptr, indices, rows, cols,
-                                                                                      nnz, br, bc, min_nnz, ns, w);
+                                                                                      nnz, br, bc, min_nnz, ns, w, rec);
         GL_LAUNCH_CHECK("build_count_kernel");
         const int64_t ncb = ceil_div(cols, bc);
         int64_t big_blocks = (int64_t)num_sms() * GL_BUILD_COUNT_BIG_CTAS;
@@ -1550,7 +1579,7 @@ int fill_impl(const I* indptr, const I* indices, const S* values, int64_t rows, 
 #define GL_FILL_LAUNCH(G)                                                                                        \
     build_fill_kernel<I, S, G><<<(unsigned)blocks, kBuildThreads, 0, stream>>>(                                   \
         indptr, indices, values, rows, cols, nnz, br, bc, min_nnz, ns, (int64_t)ncb, sizeof(I) == 4, nchain, w,   \
-        codes, coords, offsets, data, rem_col, rem_val, stripe_ptr)
+        codes, coords, offsets, data, rem_col, rem_val, stripe_ptr, ncb < (uint64_t)INT32_MAX)
         if (br <= 8 && GL_BUILD_FILL_GROUP <= 8) GL_FILL_LAUNCH(8);
         else if (br <= 16 && GL_BUILD_FILL_GROUP <= 16) GL_FILL_LAUNCH(16);
         else GL_FILL_LAUNCH(32);
