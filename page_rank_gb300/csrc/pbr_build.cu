@@ -3,23 +3,27 @@
 // csr_to_pbr<index_t, scalar_t> (Backend/graph_link/pbr_matrix/pbr_matrix.cpp:
 // 340-477) for canonical CSR input.
 //
-// Work split: one warp per stripe (block_rows consecutive rows).  Lane r walks
-// row r of the stripe; because each row is column-sorted, the warp merges the
-// rows by block column (warp-min of the lanes' head block columns), which
-// yields the stripe's distinct blocks in block-column order together with
-// their bitmask, the CSR position of their first nonzero, and per-row counts.
-// Warps draw their stripes from a counter.  Long stripes (more than
+// Work split: a group of lanes per stripe (block_rows consecutive rows; four
+// 8-lane groups per warp for blocks up to 8 rows).  Lane r walks row r of the
+// stripe; because each row is column-sorted, the group merges the rows by
+// block column (the minimum of the lanes' head block columns), which yields
+// the stripe's distinct blocks in block-column order together with their
+// bitmask, the CSR position of their first nonzero, and per-row counts.
+// Groups draw their stripes from a counter.  Long stripes (more than
 // kBigCountEntries entries to count, more than kSmallStripeBlocks distinct
-// blocks to order) go to 1024-thread CTAs instead, which sort instead of
-// merging; the count pass lists them for those kernels, hub stripes first.
+// blocks to order) go to 1024-thread CTAs instead, which sort (or, in shared
+// memory, rank) instead of merging; the count pass lists them for those
+// kernels, hub stripes first.
 //
 // Three device passes:
 //   count  — per stripe: distinct / kept blocks, packed values; per row:
 //            remainder entries; CSR validation (range, strictly increasing);
+//            the block records of merged stripes and the sorted order of
+//            long ones are left in the workspace for the fill;
 //   (scans of those counts; an exclusive running max of distinct blocks)
-//   fill   — per stripe: record the blocks, reproduce the reference's emit
-//            order (below), write codes / coords / offsets, then merge once
-//            more to move the values into block_data or the remainder.
+//   fill   — per stripe: take the blocks' records, reproduce the reference's
+//            emit order (below), write codes / coords / offsets, then merge
+//            once more to move the values into block_data or the remainder.
 //
 // Emit order.  The reference emits a stripe's kept blocks in the iteration
 // order of a std::unordered_map<index_t, ...> keyed by the block index
